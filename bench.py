@@ -1,0 +1,526 @@
+#!/usr/bin/env python
+"""Benchmark: mixed-precision (FP32 factor + FP64 refinement) vs plain FP64
+compact SPD solves on one or more GB300s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cbk|reference]
+
+Workload (the mixed-precision dposv configuration): for each n in
+{8, 16, 32, 48}, 262,144 SPD matrices A = U diag(s) U^T (U Haar-random, the Q
+of a seeded Gaussian's QR with R's diagonal signs folded in; s log-uniform
+from 1 to 1/kappa, log10 kappa uniform in [1, 6]), one right-hand side
+b ~ N(0,1), compact layout with V = 32, column-major, lower triangle. A step
+solves all four batches (1,048,576 systems). Synthetic data stands in for a
+dataset; the seed is in the JSON line.
+
+value      refined solves/s with the inputs resident in HBM (CUDA events around
+           the solve launches; inputs restored and L2 flushed untimed before
+           every step); the plain FP64 dposv_compact is timed the same way on
+           the same matrices and both paths' worst normwise backward error is
+           reported against the common bound 8 n eps64 ("equal FP64 error")
+e2e        the same solves through the C ABI from pinned host buffers: the H2D
+           copy of every A and b, the solves and the D2H copy of every x inside
+           the timed region
+roofline   HBM roofline of the dominant launch (the largest order): algorithmic
+           bytes (lower triangle of A read once, b read, x written) over its
+           measured duration; fp64_pipe the same launch's FP64 work over the
+           measured FP64 FMA rate -- the pipe that binds on this part
+cpu_baseline  the oracle (the C restatement of the reference's dposv_compact,
+           -O3, OpenMP over groups of V = 8, every host core) on a bounded
+           sample of the same workload
+
+With --gpus N > 1 (torchrun, one rank per GPU) every rank solves its own full
+replica of the workload: value = all ranks' solves / the slowest rank's time.
+--impl reference times the CPU implementation instead (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s & HBM GB/s, n=8-48: refined FP32 vs plain FP64 at equal FP64 error"
+UNIT = "solves/s"
+SIZES = (8, 16, 32, 48)
+NM = 262144
+V = 32
+NRHS = 1
+SEED = 0x5EED
+LOG10_KAPPA = (1.0, 6.0)
+CPU_SAMPLE = 16384  # matrices per order in the CPU timing sample
+WORKLOAD = ("mixed-precision dposv_compact: n in {8,16,32,48}, nrhs=1, 262144 SPD matrices "
+            "per n (kappa log-uniform 1e1..1e6), compact V=32 column-major lower")
+DATA = ("synthetic (seed 0x5EED): A = U diag(s) U^T, U Haar (sign-fixed QR of a Gaussian), "
+        "s log-uniform with log10 kappa ~ U[1,6]; b ~ N(0,1)")
+
+
+def bytes_per_matrix(n: int) -> int:
+    """Algorithmic HBM bytes of one solve: the lower triangle of A read once,
+    b read and x written (FP64)."""
+    return 8 * (n * (n + 1) // 2 + 2 * n * NRHS)
+
+
+def plain_flops(n: int) -> float:
+    """FP64 flops of the plain factor + solve: n^3/3 + n^2/2 + n/6 + 2 n^2 nrhs."""
+    return n ** 3 / 3 + n * n / 2 + n / 6 + 2 * n * n * NRHS
+
+
+# ---------------------------------------------------------------------------
+# process setup
+# ---------------------------------------------------------------------------
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region (clocks, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.idx)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU implementation (the reference arm, and the cpu_baseline of ours)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(seed=SEED, per_n=CPU_SAMPLE):
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases as C
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    data = []
+    for n in SIZES:
+        A, _ = C.gen_spd_cond(rng, per_n, n, LOG10_KAPPA)
+        B = rng.standard_normal((per_n, n, NRHS))
+        data.append((n, O.pack(A, 8), O.pack(B, 8, pad_diag=0.0)))
+    return data
+
+
+def cpu_time_step(lib, data):
+    """One pass over the sample with the reference's dposv_compact (V = 8,
+    the AVX-512 / two-NEON-register double width); returns seconds."""
+    import numpy as np
+    work = [(n, a.copy(), b.copy()) for n, a, b in data]
+    t0 = time.perf_counter()
+    for n, a, b in work:
+        info = lib.call("posv", np.float64, "C", "L", n, NRHS, a, n, b, n, 8, CPU_SAMPLE)
+        assert info == 0
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(steps=3):
+    from oracle import oracle as O
+    lib = O.oracle(fast=True)
+    data = cpu_sample()
+    cpu_time_step(lib, data)  # warm-up
+    best = min(cpu_time_step(lib, data) for _ in range(steps))
+    solves = CPU_SAMPLE * len(SIZES)
+    return {"value": solves / best, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            "sample": (f"{CPU_SAMPLE} matrices per n in {{8,16,32,48}} from the same "
+                       f"distribution, dposv_compact V=8, best of {steps} passes "
+                       f"({best * 1e3:.1f} ms per pass)")}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    lib = O.oracle(fast=True)
+    data = cpu_sample()
+    for _ in range(args.warmup):
+        cpu_time_step(lib, data)
+    times = [cpu_time_step(lib, data) for _ in range(args.steps)]
+    solves = CPU_SAMPLE * len(SIZES)
+    value = solves * args.steps / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD, "sample_per_n": CPU_SAMPLE, "V": 8,
+                   "threads": O.max_threads()},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                         "sample": f"{CPU_SAMPLE} matrices per n, every step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+
+def gen_batch(n, nm, gen, device):
+    """Dense A (nm, n, n) FP64 on the device and b (nm, n, 1), as the docstring
+    describes."""
+    import torch
+    f64 = torch.float64
+    G = torch.randn(nm, n, n, dtype=f64, device=device, generator=gen)
+    Q, R = torch.linalg.qr(G)
+    d = torch.sign(torch.diagonal(R, dim1=1, dim2=2))
+    d[d == 0] = 1
+    U = Q * d[:, None, :]
+    del G, Q, R
+    lk = torch.empty(nm, dtype=f64, device=device).uniform_(*LOG10_KAPPA, generator=gen)
+    u = torch.sort(torch.rand(nm, n, dtype=f64, device=device, generator=gen), dim=1).values
+    if n > 1:
+        u[:, 0] = 0
+        u[:, -1] = 1
+    s = torch.pow(10.0, -lk[:, None] * u)
+    A = (U * s[:, None, :]) @ U.transpose(1, 2)
+    del U
+    A = torch.tril(A) + torch.tril(A, -1).transpose(1, 2)
+    B = torch.randn(nm, n, NRHS, dtype=f64, device=device, generator=gen)
+    return A, B
+
+
+def pack_dev(cbk, M):
+    """Dense (nm, r, c) FP64 -> compact V=32 column-major, on the device."""
+    import torch
+    nm, r, c = M.shape
+    ng = (nm + V - 1) // V
+    out = torch.empty(ng * r * c * V, dtype=M.dtype, device=M.device)
+    colmajor = M.transpose(1, 2).contiguous()
+    pad = 1.0 if r == c else 0.0
+    cbk.check("pack", cbk.call("d", "pack", "C", r, c, colmajor, r, r * c, out, r, V, nm, pad))
+    return out
+
+
+def x_dense(bp, n, nm):
+    """Compact (V=32, col-major, ld=n) n x 1 batch -> dense (nm, n, 1)."""
+    ng = (nm + V - 1) // V
+    return bp.view(ng, n, V).permute(0, 2, 1).reshape(ng * V, n)[:nm].unsqueeze(2)
+
+
+def berr_max(A, X, B):
+    """Largest normwise backward error over the batch, FP64 on the device."""
+    import torch
+    R = B - torch.bmm(A, X)
+    an = A.abs().sum(dim=2).amax(dim=1)
+    rn = R.abs().amax(dim=(1, 2))
+    xn = X.abs().amax(dim=(1, 2))
+    bn = B.abs().amax(dim=(1, 2))
+    return float((rn / (an * xn + bn)).max())
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import cbk_gb300 as cbk
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + rank)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    batches = []
+    for n in SIZES:
+        A, B = gen_batch(n, NM, gen, dev)
+        ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+        batches.append(dict(n=n, A=A, B=B, ap0=ap0, bp0=bp0, ap=torch.empty_like(ap0),
+                            bp=torch.empty_like(bp0),
+                            work=torch.empty(max(1, cbk.dposv_refined_lwork(n, NRHS, V, NM)),
+                                             dtype=torch.uint8, device=dev),
+                            iters=torch.empty(NM, dtype=torch.int32, device=dev),
+                            berr=torch.empty(NM, dtype=torch.float64, device=dev)))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB of L2
+    torch.cuda.synchronize()
+
+    def refined(b):
+        return cbk.dposv_refined_compact("C", "L", b["n"], NRHS, b["ap"], b["n"], b["bp"], b["n"],
+                                         V, NM, 10, b["iters"], b["berr"], b["work"])
+
+    def plain(b):
+        return cbk.dposv_compact("C", "L", b["n"], NRHS, b["ap"], b["n"], b["bp"], b["n"], V, NM)
+
+    def restore():
+        for b in batches:
+            b["ap"].copy_(b["ap0"])
+            b["bp"].copy_(b["bp0"])
+        flush.fill_(1)
+
+    def step(fn):
+        """One timed step: per-launch events; returns (total ms, [ms per n])."""
+        restore()
+        torch.cuda.synchronize()
+        barrier()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(batches) + 1)]
+        ev[0].record()
+        for k, b in enumerate(batches):
+            info = fn(b)
+            assert info == 0, info
+            ev[k + 1].record()
+        torch.cuda.synchronize()
+        barrier()
+        per = [ev[k].elapsed_time(ev[k + 1]) for k in range(len(batches))]
+        return ev[0].elapsed_time(ev[-1]), per
+
+    def run_path(fn, K, W):
+        for _ in range(W):
+            step(fn)
+        tot, per = [], []
+        for _ in range(K):
+            t, p = step(fn)
+            tot.append(t)
+            per.append(p)
+        return tot, per
+
+    # the headline path, with the clocks sampled over its timed steps
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
+    for _ in range(args.warmup):
+        step(refined)
+    with Clocks(gpu_index) as clk:
+        ref_tot, ref_per = run_path(refined, args.steps, 0)
+    clocks = clk.summary()
+    # outcomes of the refined path (from the last step) and its backward error
+    ref_stats = {}
+    worst_ref = 0.0
+    for b in batches:
+        it = b["iters"]
+        conv = it >= 0
+        ref_stats[b["n"]] = {
+            "converged_frac": float(conv.float().mean()),
+            "mean_corrections": float(it[conv].float().mean()) if bool(conv.any()) else None,
+            "fallbacks": {str(c): int((it == c).sum()) for c in (-1, -2, -3)},
+        }
+        e = berr_max(b["A"], x_dense(b["bp"], b["n"], NM), b["B"])
+        ref_stats[b["n"]]["max_berr_over_n_eps"] = e / (b["n"] * 2.220446049250313e-16)
+        worst_ref = max(worst_ref, ref_stats[b["n"]]["max_berr_over_n_eps"])
+    # the plain FP64 path on the same matrices
+    pl_tot, pl_per = run_path(plain, args.steps, max(1, args.warmup // 2))
+    worst_plain = 0.0
+    for b in batches:
+        e = berr_max(b["A"], x_dense(b["bp"], b["n"], NM), b["B"])
+        ref_stats[b["n"]]["plain_max_berr_over_n_eps"] = e / (b["n"] * 2.220446049250313e-16)
+        worst_plain = max(worst_plain, ref_stats[b["n"]]["plain_max_berr_over_n_eps"])
+
+    solves = NM * len(SIZES)
+    t_ref = sum(ref_tot) / len(ref_tot)
+    t_pl = sum(pl_tot) / len(pl_tot)
+    # slowest rank decides
+    if ws > 1:
+        tt = torch.tensor([t_ref, t_pl], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ref, t_pl = float(tt[0]), float(tt[1])
+    value = ws * solves / (t_ref * 1e-3)
+    plain_value = ws * solves / (t_pl * 1e-3)
+
+    per_n = {}
+    for k, b in enumerate(batches):
+        n = b["n"]
+        r_ms = statistics.mean(p[k] for p in ref_per)
+        p_ms = statistics.mean(p[k] for p in pl_per)
+        per_n[str(n)] = dict(ref_stats[n], refined_ms=r_ms, plain_ms=p_ms,
+                             speedup=p_ms / r_ms,
+                             refined_gbs=NM * bytes_per_matrix(n) / (r_ms * 1e-3) / 1e9,
+                             plain_gbs=NM * bytes_per_matrix(n) / (p_ms * 1e-3) / 1e9)
+
+    # roofline of the dominant launch (the longest: the largest order)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    kdom = max(range(len(batches)), key=lambda k: statistics.mean(p[k] for p in ref_per))
+    ndom = batches[kdom]["n"]
+    dom_ms = statistics.mean(p[kdom] for p in ref_per)
+    achieved = NM * bytes_per_matrix(ndom) / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tr = json.load(f)
+        per_matrix = tr.get(f"posv_refined_n{ndom}", {}).get("dram_bytes_per_matrix")
+        traffic = per_matrix * NM if per_matrix else None
+    except (OSError, ValueError):
+        pass
+    rate = ctypes_fma_rate(cbk)
+    # FP64 work of the dominant refined launch: (corrections + 1) residuals of
+    # n^2 FMAs per right-hand side, plus the fallbacks' plain solves
+    it = batches[kdom]["iters"]
+    conv = it >= 0
+    ncorr = float(it[conv].double().sum()) + float(conv.sum())
+    nfall = int((~conv).sum())
+    fp64_flops = 2.0 * ndom * ndom * ncorr + plain_flops(ndom) * nfall
+    pl_dom_ms = statistics.mean(p[kdom] for p in pl_per)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ref, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 factor + f64 refinement (f64 results)", "data": DATA,
+        "config": {"workload": WORKLOAD, "nm_per_n": NM, "n": list(SIZES), "nrhs": NRHS, "V": V,
+                   "max_iter": 10, "l2": "flushed (256 MiB write) before every timed step",
+                   "inputs": "restored untimed before every step", "parallelism": "replicas"},
+        "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": t_pl},
+        "speedup_refined_vs_plain": plain_value and value / plain_value,
+        "equal_error": {"bound": "berr <= 8 n eps64 (normwise, inf-norm)",
+                        "refined_max_berr_over_n_eps": worst_ref,
+                        "plain_max_berr_over_n_eps": worst_plain,
+                        "both_within_bound": worst_ref <= 8 and worst_plain <= 8},
+        "per_n": per_n,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "kernel": f"k_posv_refined (n={ndom})",
+                     "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)"},
+        "fp64_pipe": {"kernel": f"k_posv_refined (n={ndom})", "unit": "TFLOP/s",
+                      "achieved": fp64_flops / (dom_ms * 1e-3) / 1e12,
+                      "plain_achieved": NM * plain_flops(ndom) / (pl_dom_ms * 1e-3) / 1e12,
+                      "peak": rate, "peak_source": "measured FP64 FMA rate "
+                      "(cbk_cuda_measure_fma_rate, this run)"},
+        "gpu_launches": len(SIZES) * args.steps,
+        "clocks": clocks,
+    }
+    if ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    if not args.no_e2e:
+        line["e2e"] = e2e(args, cbk, batches, barrier, ws)
+    # free the device before printing
+    del batches
+    torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def ctypes_fma_rate(cbk):
+    import ctypes
+    out = ctypes.c_double(0)
+    f = cbk.lib().cbk_cuda_measure_fma_rate
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    f.restype = ctypes.c_int
+    return out.value if f(1, ctypes.byref(out)) == 0 else None
+
+
+def e2e(args, cbk, batches, barrier, ws):
+    """The solves through the public C ABI from pinned host memory: H2D of A
+    and b, the refined solve, D2H of x, all inside the timed region."""
+    import torch
+    host = []
+    for b in batches:
+        host.append(dict(ap=b["ap0"].cpu().pin_memory(), bp=b["bp0"].cpu().pin_memory(),
+                         xp=torch.empty_like(b["bp0"], device="cpu").pin_memory()))
+    h2d = sum(h["ap"].numel() * 8 + h["bp"].numel() * 8 for h in host)
+    d2h = sum(h["xp"].numel() * 8 for h in host)
+
+    def one():
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for b, h in zip(batches, host):
+            b["ap"].copy_(h["ap"], non_blocking=True)
+            b["bp"].copy_(h["bp"], non_blocking=True)
+            info = cbk.dposv_refined_compact("C", "L", b["n"], NRHS, b["ap"], b["n"], b["bp"],
+                                             b["n"], V, NM, 10, None, None, b["work"])
+            assert info == 0, info
+            h["xp"].copy_(b["bp"], non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        return e0.elapsed_time(e1)
+
+    for _ in range(max(1, args.warmup // 2)):
+        one()
+    ts = [one() for _ in range(args.steps)]
+    t = sum(ts) / len(ts)
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t], dtype=torch.float64, device=batches[0]["ap"].device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt[0])
+    return {"value": ws * NM * len(SIZES) / (t * 1e-3), "unit": UNIT, "ms_per_step": t,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "path": "cudaMemcpyAsync H2D (pinned) -> cbk_cuda_dposv_refined_compact_async -> "
+                    "D2H, per n"}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("cbk", "reference"), default="cbk")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3  # at least three untimed warm-up steps
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,433 @@
+// cbk_api.cpp -- the extern "C" entry points of include/cbk_cuda.h.
+//
+// Each routine checks its arguments in argument order and returns -j for the
+// first illegal one, takes the reference's quick returns, then enqueues the
+// CUDA kernel(s) on the caller's stream. The checks and quick returns restate
+// the reference's C adapter, src/cbk.cpp:46-320 (per-routine templates geqrf
+// :61-78, ormqr :80-105, orgqr :107-127, potrf :129-147, sytrfnp :149-167,
+// sym_solve_args :173-188, potrs :190-205, posv :207-224, sytrsnp :226-241,
+// sysvnp :243-260, trsm :262-293, gels :295-320), with the accepted interleave
+// widths widened to multiples of 32. Pointers are never inspected.
+#include "../../include/cbk_cuda.h"
+#include "cbk_launch.h"
+
+#include <cuda_runtime.h>
+
+namespace {
+
+using namespace cbkcuda;
+
+inline bool opt(char c, char upper)
+{
+    return c == upper || c == upper + ('a' - 'A');
+}
+
+inline int max1(int x)
+{
+    return x < 1 ? 1 : x;
+}
+
+inline bool vlen_ok(int V)
+{
+    if (V == 2 || V == 4 || V == 8 || V == 16) return true;
+    return V >= 32 && V <= 1024 && V % 32 == 0;
+}
+
+inline int cuda_status(cudaError_t e)
+{
+    return e == cudaSuccess ? 0 : CBK_CUDA_ERROR_BASE + (int)e;
+}
+
+template <typename T>
+int geqrf(char layout, int m, int n, T *ap, int ldap, T *taup, int V, int nm, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    if (!col && !row) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (ldap < max1(row ? n : m)) return -5;
+    if (!vlen_ok(V)) return -7;
+    if (nm < 0) return -8;
+    if (m == 0 || n == 0 || nm == 0) return 0;
+    return cuda_status(launch_geqrf<T>(row, m, n, ap, ldap, taup, V, nm, s));
+}
+
+template <typename T>
+int ormqr(char layout, char side, char trans, int m, int n, int k, const T *ap, int ldap,
+          const T *taup, T *cp, int ldcp, int V, int nm, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const bool left = opt(side, 'L'), right = opt(side, 'R');
+    const int nq = left ? m : n;
+    if (!col && !row) return -1;
+    if (!left && !right) return -2;
+    if (!opt(trans, 'T') && !opt(trans, 'N')) return -3;
+    if (m < 0) return -4;
+    if (n < 0) return -5;
+    if (k < 0 || k > nq) return -6;
+    if (ldap < max1(row ? k : nq)) return -8;
+    if (ldcp < max1(row ? n : m)) return -11;
+    if (!vlen_ok(V)) return -12;
+    if (nm < 0) return -13;
+    if (m == 0 || n == 0 || k == 0 || nm == 0) return 0;
+    return cuda_status(launch_ormqr<T>(left, row, opt(trans, 'T'), m, n, k, ap, ldap, taup, cp,
+                                       ldcp, V, nm, s));
+}
+
+template <typename T>
+int orgqr(char layout, int m, int n, int k, T *ap, int ldap, const T *taup, int V, int nm,
+          cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    if (!col && !row) return -1;
+    if (m < 0) return -2;
+    if (n < 0 || n > m) return -3;
+    if (k < 0 || k > n) return -4;
+    if (ldap < max1(row ? n : m)) return -6;
+    if (!vlen_ok(V)) return -8;
+    if (nm < 0) return -9;
+    // k == 0 is not empty: Q = I(:, 0:n-1) is still written
+    if (m == 0 || n == 0 || nm == 0) return 0;
+    return cuda_status(launch_orgqr<T>(row, m, n, k, ap, ldap, taup, V, nm, s));
+}
+
+template <typename T>
+int factor(bool ldlt, char layout, char uplo, int n, T *ap, int ldap, int V, int nm,
+           cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const bool lo = opt(uplo, 'L'), up = opt(uplo, 'U');
+    if (!col && !row) return -1;
+    if (!lo && !up) return -2;
+    if (n < 0) return -3;
+    if (ldap < max1(n)) return -5;
+    if (!vlen_ok(V)) return -6;
+    if (nm < 0) return -7;
+    if (n == 0 || nm == 0) return 0;
+    return cuda_status(launch_factor<T>(ldlt, row, up, n, ap, ldap, V, nm, s));
+}
+
+// ?potrs / ?posv / ?sytrsnp / ?sysvnp share one signature and one check
+// (sym_solve_args): -1 layout -2 uplo -3 n -4 nrhs -6 ldap -8 ldbp -9 V -10 nm.
+int sym_solve_args(char layout, char uplo, int n, int nrhs, int ldap, int ldbp, int V, int nm,
+                   bool &row, bool &up)
+{
+    const bool col = opt(layout, 'C'), lo = opt(uplo, 'L');
+    row = opt(layout, 'R');
+    up = opt(uplo, 'U');
+    if (!col && !row) return -1;
+    if (!lo && !up) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (ldap < max1(n)) return -6;
+    if (ldbp < max1(row ? nrhs : n)) return -8;
+    if (!vlen_ok(V)) return -9;
+    if (nm < 0) return -10;
+    return 0;
+}
+
+template <typename T>
+int sym_solve(bool ldlt, bool fused, char layout, char uplo, int n, int nrhs, T *ap, int ldap,
+              T *bp, int ldbp, int V, int nm, cudaStream_t s)
+{
+    bool row, up;
+    if (int e = sym_solve_args(layout, uplo, n, nrhs, ldap, ldbp, V, nm, row, up)) return e;
+    if (n == 0 || nm == 0) return 0;
+    if (nrhs == 0) {
+        // the solve alone has nothing to do; the fused driver still factors
+        // (LAPACK ?posv / ?sysv), never referencing bp
+        if (!fused) return 0;
+        return cuda_status(launch_factor<T>(ldlt, row, up, n, ap, ldap, V, nm, s));
+    }
+    return cuda_status(
+        launch_sym_solve<T>(ldlt, fused, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, s));
+}
+
+template <typename T>
+int trsm(char layout, char side, char uplo, char transa, char diag, int m, int n, T alpha,
+         const T *ap, int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const bool left = opt(side, 'L'), right = opt(side, 'R');
+    const bool up = opt(uplo, 'U'), lo = opt(uplo, 'L');
+    const bool tran = opt(transa, 'T') || opt(transa, 'C');
+    const bool unit = opt(diag, 'U');
+    const int sdim = left ? m : n;
+    if (!col && !row) return -1;
+    if (!left && !right) return -2;
+    if (!up && !lo) return -3;
+    if (!tran && !opt(transa, 'N')) return -4;
+    if (!unit && !opt(diag, 'N')) return -5;
+    if (m < 0) return -6;
+    if (n < 0) return -7;
+    // -8 alpha: every value is legal (0 means B := 0)
+    if (ldap < max1(sdim)) return -10;
+    if (ldbp < max1(row ? n : m)) return -12;
+    if (!vlen_ok(V)) return -13;
+    if (nm < 0) return -14;
+    if (m == 0 || n == 0 || nm == 0) return 0;
+    if (alpha == T(0)) return cuda_status(launch_zero<T>(row, m, n, bp, ldbp, V, nm, s));
+    return cuda_status(
+        launch_trsm<T>(left, up, row, tran, unit, m, n, alpha, ap, ldap, bp, ldbp, V, nm, s));
+}
+
+template <typename T>
+int gels(char layout, char trans, int m, int n, int nrhs, T *ap, int ldap, T *bp, int ldbp,
+         T *taup, int V, int nm, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const int mx = m > n ? m : n;
+    if (!col && !row) return -1;
+    if (!opt(trans, 'N') && !opt(trans, 'T') && !opt(trans, 'C')) return -2;
+    if (m < 0) return -3;
+    if (n < 0) return -4;
+    if (nrhs < 0) return -5;
+    if (ldap < max1(row ? n : m)) return -7;
+    if (ldbp < max1(row ? nrhs : mx)) return -9;
+    if (!vlen_ok(V)) return -11;
+    if (nm < 0) return -12;
+    if (nrhs == 0 || nm == 0 || mx == 0) return 0;
+    const bool tran = opt(trans, 'T') || opt(trans, 'C');
+    return cuda_status(
+        launch_gels<T>(row, tran, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, s));
+}
+
+template <typename T>
+int pack(char layout, int m, int n, const T *a, int lda, long long stride, T *ap, int ldap,
+         int V, int nm, T pad_diag, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    if (!col && !row) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (lda < max1(row ? n : m)) return -5;
+    if (stride < (long long)lda * (row ? m : n)) return -6;
+    if (ldap < max1(row ? n : m)) return -8;
+    if (!vlen_ok(V)) return -9;
+    if (nm < 0) return -10;
+    if (m == 0 || n == 0 || nm == 0) return 0;
+    return cuda_status(launch_pack<T>(row, m, n, a, lda, stride, ap, ldap, V, nm, pad_diag, s));
+}
+
+template <typename T>
+int unpack(char layout, int m, int n, const T *ap, int ldap, T *a, int lda, long long stride,
+           int V, int nm, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    if (!col && !row) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (ldap < max1(row ? n : m)) return -5;
+    if (lda < max1(row ? n : m)) return -7;
+    if (stride < (long long)lda * (row ? m : n)) return -8;
+    if (!vlen_ok(V)) return -9;
+    if (nm < 0) return -10;
+    if (m == 0 || n == 0 || nm == 0) return 0;
+    return cuda_status(launch_unpack<T>(row, m, n, ap, ldap, a, lda, stride, V, nm, s));
+}
+
+int posv_refined(char layout, char uplo, int n, int nrhs, double *ap, int ldap, double *bp,
+                 int ldbp, int V, int nm, int max_iter, int *iters, double *berr, void *work,
+                 long long lwork, cudaStream_t s)
+{
+    bool row, up;
+    if (int e = sym_solve_args(layout, uplo, n, nrhs, ldap, ldbp, V, nm, row, up)) return e;
+    if (max_iter < 0) return -11;
+    if (n == 0 || nm == 0 || nrhs == 0) return 0;
+    const size_t need = posv_refined_lwork(n, nrhs, V, nm);
+    if (need > 0 && (work == nullptr || lwork < (long long)need)) return -15;
+    return cuda_status(launch_posv_refined(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter,
+                                           iters, berr, work, s));
+}
+
+inline cudaStream_t S(cbk_stream_t s)
+{
+    return reinterpret_cast<cudaStream_t>(s);
+}
+
+} // namespace
+
+extern "C" {
+
+int cbk_cuda_get_version(void)
+{
+    return CBK_CUDA_VERSION;
+}
+
+int cbk_cuda_vlen_ok(int V)
+{
+    return vlen_ok(V) ? 1 : 0;
+}
+
+const char *cbk_cuda_status_string(int info)
+{
+    if (info == 0) return "success";
+    if (info < 0) return "illegal argument (the -info-th)";
+    if (info >= CBK_CUDA_ERROR_BASE)
+        return cudaGetErrorString((cudaError_t)(info - CBK_CUDA_ERROR_BASE));
+    return "unknown status";
+}
+
+// One definition per routine and scalar type: NAME_async with the stream and
+// NAME on the legacy default stream.
+#define CBK_CUDA_ENTRY_POINTS(T, p)                                                               \
+    int cbk_cuda_##p##geqrf_compact_async(char layout, int m, int n, T *ap, int ldap, T *taup,    \
+                                          int V, int nm, cbk_stream_t st)                         \
+    {                                                                                             \
+        return geqrf<T>(layout, m, n, ap, ldap, taup, V, nm, S(st));                              \
+    }                                                                                             \
+    int cbk_cuda_##p##geqrf_compact(char layout, int m, int n, T *ap, int ldap, T *taup, int V,   \
+                                    int nm)                                                       \
+    {                                                                                             \
+        return geqrf<T>(layout, m, n, ap, ldap, taup, V, nm, 0);                                  \
+    }                                                                                             \
+    int cbk_cuda_##p##ormqr_compact_async(char layout, char side, char trans, int m, int n,       \
+                                          int k, const T *ap, int ldap, const T *taup, T *cp,     \
+                                          int ldcp, int V, int nm, cbk_stream_t st)               \
+    {                                                                                             \
+        return ormqr<T>(layout, side, trans, m, n, k, ap, ldap, taup, cp, ldcp, V, nm, S(st));    \
+    }                                                                                             \
+    int cbk_cuda_##p##ormqr_compact(char layout, char side, char trans, int m, int n, int k,      \
+                                    const T *ap, int ldap, const T *taup, T *cp, int ldcp, int V, \
+                                    int nm)                                                       \
+    {                                                                                             \
+        return ormqr<T>(layout, side, trans, m, n, k, ap, ldap, taup, cp, ldcp, V, nm, 0);        \
+    }                                                                                             \
+    int cbk_cuda_##p##orgqr_compact_async(char layout, int m, int n, int k, T *ap, int ldap,      \
+                                          const T *taup, int V, int nm, cbk_stream_t st)          \
+    {                                                                                             \
+        return orgqr<T>(layout, m, n, k, ap, ldap, taup, V, nm, S(st));                           \
+    }                                                                                             \
+    int cbk_cuda_##p##orgqr_compact(char layout, int m, int n, int k, T *ap, int ldap,            \
+                                    const T *taup, int V, int nm)                                 \
+    {                                                                                             \
+        return orgqr<T>(layout, m, n, k, ap, ldap, taup, V, nm, 0);                               \
+    }                                                                                             \
+    int cbk_cuda_##p##potrf_compact_async(char layout, char uplo, int n, T *ap, int ldap, int V,  \
+                                          int nm, cbk_stream_t st)                                \
+    {                                                                                             \
+        return factor<T>(false, layout, uplo, n, ap, ldap, V, nm, S(st));                         \
+    }                                                                                             \
+    int cbk_cuda_##p##potrf_compact(char layout, char uplo, int n, T *ap, int ldap, int V,        \
+                                    int nm)                                                       \
+    {                                                                                             \
+        return factor<T>(false, layout, uplo, n, ap, ldap, V, nm, 0);                             \
+    }                                                                                             \
+    int cbk_cuda_##p##sytrfnp_compact_async(char layout, char uplo, int n, T *ap, int ldap,       \
+                                            int V, int nm, cbk_stream_t st)                       \
+    {                                                                                             \
+        return factor<T>(true, layout, uplo, n, ap, ldap, V, nm, S(st));                          \
+    }                                                                                             \
+    int cbk_cuda_##p##sytrfnp_compact(char layout, char uplo, int n, T *ap, int ldap, int V,      \
+                                      int nm)                                                     \
+    {                                                                                             \
+        return factor<T>(true, layout, uplo, n, ap, ldap, V, nm, 0);                              \
+    }                                                                                             \
+    int cbk_cuda_##p##potrs_compact_async(char layout, char uplo, int n, int nrhs, const T *ap,   \
+                                          int ldap, T *bp, int ldbp, int V, int nm,               \
+                                          cbk_stream_t st)                                        \
+    {                                                                                             \
+        return sym_solve<T>(false, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap, bp,   \
+                            ldbp, V, nm, S(st));                                                  \
+    }                                                                                             \
+    int cbk_cuda_##p##potrs_compact(char layout, char uplo, int n, int nrhs, const T *ap,         \
+                                    int ldap, T *bp, int ldbp, int V, int nm)                     \
+    {                                                                                             \
+        return sym_solve<T>(false, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap, bp,   \
+                            ldbp, V, nm, 0);                                                      \
+    }                                                                                             \
+    int cbk_cuda_##p##posv_compact_async(char layout, char uplo, int n, int nrhs, T *ap,          \
+                                         int ldap, T *bp, int ldbp, int V, int nm,                \
+                                         cbk_stream_t st)                                         \
+    {                                                                                             \
+        return sym_solve<T>(false, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm,        \
+                            S(st));                                                               \
+    }                                                                                             \
+    int cbk_cuda_##p##posv_compact(char layout, char uplo, int n, int nrhs, T *ap, int ldap,      \
+                                   T *bp, int ldbp, int V, int nm)                                \
+    {                                                                                             \
+        return sym_solve<T>(false, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, 0);    \
+    }                                                                                             \
+    int cbk_cuda_##p##sytrsnp_compact_async(char layout, char uplo, int n, int nrhs,              \
+                                            const T *ap, int ldap, T *bp, int ldbp, int V,        \
+                                            int nm, cbk_stream_t st)                              \
+    {                                                                                             \
+        return sym_solve<T>(true, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap, bp,    \
+                            ldbp, V, nm, S(st));                                                  \
+    }                                                                                             \
+    int cbk_cuda_##p##sytrsnp_compact(char layout, char uplo, int n, int nrhs, const T *ap,       \
+                                      int ldap, T *bp, int ldbp, int V, int nm)                   \
+    {                                                                                             \
+        return sym_solve<T>(true, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap, bp,    \
+                            ldbp, V, nm, 0);                                                      \
+    }                                                                                             \
+    int cbk_cuda_##p##sysvnp_compact_async(char layout, char uplo, int n, int nrhs, T *ap,        \
+                                           int ldap, T *bp, int ldbp, int V, int nm,              \
+                                           cbk_stream_t st)                                       \
+    {                                                                                             \
+        return sym_solve<T>(true, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, S(st)); \
+    }                                                                                             \
+    int cbk_cuda_##p##sysvnp_compact(char layout, char uplo, int n, int nrhs, T *ap, int ldap,    \
+                                     T *bp, int ldbp, int V, int nm)                              \
+    {                                                                                             \
+        return sym_solve<T>(true, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, 0);     \
+    }                                                                                             \
+    int cbk_cuda_##p##trsm_compact_async(char layout, char side, char uplo, char transa,          \
+                                         char diag, int m, int n, T alpha, const T *ap, int ldap, \
+                                         T *bp, int ldbp, int V, int nm, cbk_stream_t st)         \
+    {                                                                                             \
+        return trsm<T>(layout, side, uplo, transa, diag, m, n, alpha, ap, ldap, bp, ldbp, V, nm,  \
+                       S(st));                                                                    \
+    }                                                                                             \
+    int cbk_cuda_##p##trsm_compact(char layout, char side, char uplo, char transa, char diag,     \
+                                   int m, int n, T alpha, const T *ap, int ldap, T *bp, int ldbp, \
+                                   int V, int nm)                                                 \
+    {                                                                                             \
+        return trsm<T>(layout, side, uplo, transa, diag, m, n, alpha, ap, ldap, bp, ldbp, V, nm,  \
+                       0);                                                                        \
+    }                                                                                             \
+    int cbk_cuda_##p##gels_compact_async(char layout, char trans, int m, int n, int nrhs, T *ap,  \
+                                         int ldap, T *bp, int ldbp, T *taup, int V, int nm,       \
+                                         cbk_stream_t st)                                         \
+    {                                                                                             \
+        return gels<T>(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, S(st));        \
+    }                                                                                             \
+    int cbk_cuda_##p##gels_compact(char layout, char trans, int m, int n, int nrhs, T *ap,        \
+                                   int ldap, T *bp, int ldbp, T *taup, int V, int nm)             \
+    {                                                                                             \
+        return gels<T>(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, 0);            \
+    }                                                                                             \
+    int cbk_cuda_##p##pack_compact_async(char layout, int m, int n, const T *a, int lda,          \
+                                         long long stridea, T *ap, int ldap, int V, int nm,       \
+                                         T pad_diag, cbk_stream_t st)                             \
+    {                                                                                             \
+        return pack<T>(layout, m, n, a, lda, stridea, ap, ldap, V, nm, pad_diag, S(st));          \
+    }                                                                                             \
+    int cbk_cuda_##p##unpack_compact_async(char layout, int m, int n, const T *ap, int ldap,      \
+                                           T *a, int lda, long long stridea, int V, int nm,       \
+                                           cbk_stream_t st)                                       \
+    {                                                                                             \
+        return unpack<T>(layout, m, n, ap, ldap, a, lda, stridea, V, nm, S(st));                  \
+    }
+
+long long cbk_cuda_dposv_refined_compact_lwork(int n, int nrhs, int V, int nm)
+{
+    if (n < 0 || nrhs < 0 || !vlen_ok(V) || nm < 0) return -1;
+    return (long long)posv_refined_lwork(n, nrhs, V, nm);
+}
+
+int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs, double *ap,
+                                         int ldap, double *bp, int ldbp, int V, int nm,
+                                         int max_iter, int *iters, double *berr, void *work,
+                                         long long lwork, cbk_stream_t st)
+{
+    return posv_refined(layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter, iters, berr,
+                        work, lwork, S(st));
+}
+
+CBK_CUDA_ENTRY_POINTS(double, d)
+CBK_CUDA_ENTRY_POINTS(float, s)
+
+#undef CBK_CUDA_ENTRY_POINTS
+
+} // extern "C"

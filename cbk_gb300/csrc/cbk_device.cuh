@@ -1,0 +1,515 @@
+// cbk_device.cuh -- per-lane device algorithms of the compact batch kernels.
+//
+// Thread model: one CUDA thread advances one matrix of the compact batch (one
+// "lane" v of group g). Element (i,j) of V consecutive matrices is stored in V
+// adjacent scalars (include/cbk.h:22-29 of the reference), so the 32 threads
+// of a warp reading element (i,j) of 32 consecutive lanes issue one coalesced
+// 256-byte (FP64) or 128-byte (FP32) access. Every lane of the grid runs,
+// including the padded lanes of a partial last group, exactly as the
+// reference's SIMD lanes do (src/cbk_common.hpp:277-297): a padded identity
+// lane factors and solves harmlessly, and the whole buffer comes out as the
+// reference leaves it.
+//
+// The algorithms below are the reference's (right-looking, recursive-panel
+// Cholesky / LDL^T with the reordered pivot, row-dot substitution, geqr2 with
+// the branch-free larfg, dlarf sweeps, org2r), restated for one lane:
+//  * factorizations are blocked left-looking by 8-column panels: a panel's
+//    columns first take the whole rank-j0 update from the finished columns in
+//    pivot order (4 x 8 register tiles), then the in-panel rank-1 sweep --
+//    the same per-element operation sequence as the reference's recursion
+//    (src/cbk_potrf_compact.hpp:79-124, src/cbk_sytrfnp_compact.hpp:96-254);
+//  * the FP64 pipe of a GB300 SM retires about two FMAs per clock, so each
+//    element update is one fused multiply-add and repeated divides by the
+//    same pivot become one reciprocal (results then differ from the
+//    reference by rounding only, within the tests' n*eps bounds);
+//  * integer address arithmetic is free next to FP64 work and is left plain.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cbkdev {
+
+// A strided view of one lane's matrix: element (i,j) at p[i*si + j*sj], the
+// strides in scalars (the compact pack stride times V).
+template <typename T> struct LV {
+    T *p;
+    long si, sj;
+    __device__ __forceinline__ T &operator()(int i, int j) const
+    {
+        return p[(long)i * si + (long)j * sj];
+    }
+    __device__ __forceinline__ LV t() const { return {p, sj, si}; }
+};
+
+template <typename T>
+__device__ __forceinline__ LV<T> lv_make(T *p, bool row, int ld, int V)
+{
+    return row ? LV<T>{p, (long)ld * V, (long)V} : LV<T>{p, (long)V, (long)ld * V};
+}
+
+// Scalars per group of V interleaved rows x cols matrices.
+__host__ __device__ __forceinline__ size_t gstride(bool row, int ld, int rows, int cols, int V)
+{
+    return (size_t)ld * (size_t)(row ? rows : cols) * (size_t)V;
+}
+
+// The lane this thread runs: returns false past the last padded lane.
+struct Lane {
+    long g;
+    int v;
+};
+__device__ __forceinline__ bool lane_of(long ngroups, int V, Lane &ln)
+{
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ngroups * (long)V) return false;
+    ln.g = idx / V;
+    ln.v = (int)(idx - ln.g * V);
+    return true;
+}
+
+template <typename T> __device__ __forceinline__ T rcp(T x) { return T(1) / x; }
+
+// ---------------------------------------------------------------------
+// Cholesky / LDL^T of the lower triangle of a lane view
+// ---------------------------------------------------------------------
+// Every loop that issues FP64 arithmetic has compile-time bounds or exact
+// runtime bounds: a predicated-off FMA still occupies the (slow) FP64 pipe,
+// so no tile is padded.
+
+// The update of the NC panel columns j0 .. j0+NC-1 by the finished columns
+// k < j0, accumulated in pivot order (the reference's syrk tile,
+// src/cbk_sytrfnp_compact.hpp:132-173): acc -= L(i,k) * L(c,k) (Cholesky) or
+// acc -= (L(i,k) D(k)) * L(c,k) (LDL^T). The diagonal block is one
+// lower-triangular register tile; the rows below go four at a time.
+template <typename T, bool LDLT, int NC>
+__device__ void cross_panel_update_nc(int n, LV<T> A, int j0)
+{
+    {   // diagonal block: rows and columns j0 .. j0+NC-1, c <= r
+        T acc[NC][NC];
+#pragma unroll
+        for (int r = 0; r < NC; ++r)
+#pragma unroll
+            for (int c = 0; c <= r; ++c)
+                acc[r][c] = A(j0 + r, j0 + c);
+        for (int k = 0; k < j0; ++k) {
+            T l[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+                l[c] = A(j0 + c, k);
+            const T dk = LDLT ? A(k, k) : T(1);
+#pragma unroll
+            for (int r = 0; r < NC; ++r) {
+                const T li = LDLT ? l[r] * dk : l[r];
+#pragma unroll
+                for (int c = 0; c <= r; ++c)
+                    acc[r][c] = fma(-li, l[c], acc[r][c]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NC; ++r)
+#pragma unroll
+            for (int c = 0; c <= r; ++c)
+                A(j0 + r, j0 + c) = acc[r][c];
+    }
+    int i0 = j0 + NC;
+    for (; i0 + 4 <= n; i0 += 4) {
+        T acc[4][NC];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+                acc[r][c] = A(i0 + r, j0 + c);
+        for (int k = 0; k < j0; ++k) {
+            T lc[NC], li[4];
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+                lc[c] = A(j0 + c, k);
+            const T dk = LDLT ? A(k, k) : T(1);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const T l = A(i0 + r, k);
+                li[r] = LDLT ? l * dk : l;
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+                    acc[r][c] = fma(-li[r], lc[c], acc[r][c]);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+                A(i0 + r, j0 + c) = acc[r][c];
+    }
+    for (; i0 < n; ++i0) {
+        T acc[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+            acc[c] = A(i0, j0 + c);
+        for (int k = 0; k < j0; ++k) {
+            const T l = A(i0, k);
+            const T li = LDLT ? l * A(k, k) : l;
+#pragma unroll
+            for (int c = 0; c < NC; ++c)
+                acc[c] = fma(-li, A(j0 + c, k), acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+            A(i0, j0 + c) = acc[c];
+    }
+}
+
+template <typename T, bool LDLT>
+__device__ void cross_panel_update(int n, LV<T> A, int j0, int j1)
+{
+    switch (j1 - j0) {
+    case 8: cross_panel_update_nc<T, LDLT, 8>(n, A, j0); break;
+    case 7: cross_panel_update_nc<T, LDLT, 7>(n, A, j0); break;
+    case 6: cross_panel_update_nc<T, LDLT, 6>(n, A, j0); break;
+    case 5: cross_panel_update_nc<T, LDLT, 5>(n, A, j0); break;
+    case 4: cross_panel_update_nc<T, LDLT, 4>(n, A, j0); break;
+    case 3: cross_panel_update_nc<T, LDLT, 3>(n, A, j0); break;
+    case 2: cross_panel_update_nc<T, LDLT, 2>(n, A, j0); break;
+    default: cross_panel_update_nc<T, LDLT, 1>(n, A, j0); break;
+    }
+}
+
+// The in-panel rank-1 step of pivot j on the NQ panel columns to its right,
+// on the unscaled column with the weight 1/a (sytrfnp_update_block,
+// src/cbk_sytrfnp_compact.hpp:96-112): A(i,c) -= A(i,j) * (A(c,j) / a),
+// the triangular corner first, then every row below the panel.
+template <typename T, int NQ> __device__ void rank1_panel(int n, LV<T> A, int j, T inva)
+{
+    T w[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+        w[q] = A(j + 1 + q, j) * inva;
+#pragma unroll
+    for (int r = 0; r < NQ; ++r) {
+        const int i = j + 1 + r;
+        const T aij = A(i, j);
+#pragma unroll
+        for (int q = 0; q <= r; ++q)
+            A(i, j + 1 + q) = fma(-aij, w[q], A(i, j + 1 + q));
+    }
+    for (int i = j + 1 + NQ; i < n; ++i) {
+        const T aij = A(i, j);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+            A(i, j + 1 + q) = fma(-aij, w[q], A(i, j + 1 + q));
+    }
+}
+
+// The unblocked sweep of panel j0 .. j1-1 (already updated by the columns
+// left of it): per pivot the reciprocal, the in-panel rank-1 step, then the
+// sqrt and the column scaling off the pivot-to-pivot chain
+// (src/cbk_potrf_compact.hpp:79-105; src/cbk_sytrfnp_compact.hpp:216-235).
+template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int j0, int j1)
+{
+    for (int j = j0; j < j1; ++j) {
+        const T a = A(j, j);
+        const T inva = rcp(a);
+        switch (j1 - j - 1) {
+        case 7: rank1_panel<T, 7>(n, A, j, inva); break;
+        case 6: rank1_panel<T, 6>(n, A, j, inva); break;
+        case 5: rank1_panel<T, 5>(n, A, j, inva); break;
+        case 4: rank1_panel<T, 4>(n, A, j, inva); break;
+        case 3: rank1_panel<T, 3>(n, A, j, inva); break;
+        case 2: rank1_panel<T, 2>(n, A, j, inva); break;
+        case 1: rank1_panel<T, 1>(n, A, j, inva); break;
+        default: break;
+        }
+        T scale;
+        if (LDLT) {
+            scale = inva; // D(j) = a stays on the diagonal
+        }
+        else {
+            const T d = sqrt(a);
+            A(j, j) = d;
+            scale = d * inva;
+        }
+        for (int i = j + 1; i < n; ++i)
+            A(i, j) = A(i, j) * scale;
+    }
+}
+
+template <typename T, bool LDLT> __device__ void factor_lane(int n, LV<T> A)
+{
+    for (int j0 = 0; j0 < n; j0 += 8) {
+        const int j1 = min(j0 + 8, n);
+        if (j0 > 0) cross_panel_update<T, LDLT>(n, A, j0, j1);
+        panel_sweep<T, LDLT>(n, A, j0, j1);
+    }
+}
+
+// ---------------------------------------------------------------------
+// Solves from a factor held in the lower triangle of the view L
+// ---------------------------------------------------------------------
+
+// L z = B (forward) then L^T X = z (backward) on NB right-hand sides at once,
+// so every factor load feeds NB FMAs. UNIT: the diagonal holds D (LDL^T): the
+// sweeps use a unit diagonal and the D^-1 row scaling between them is folded
+// into the backward sweep's first touch of each row
+// (src/cbk_sytrsnp_compact.hpp:51-78); otherwise each row is scaled by
+// 1/L(i,i) (src/cbk_potrs_compact.hpp:46-58).
+template <typename T, bool UNIT, int NB>
+__device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0)
+{
+    for (int i = 0; i < n; ++i) {
+        T w[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            w[c] = B(i, c0 + c);
+        for (int l = 0; l < i; ++l) {
+            const T a = L(i, l);
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                w[c] = fma(-a, B(l, c0 + c), w[c]);
+        }
+        if (UNIT) {
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                B(i, c0 + c) = w[c];
+        }
+        else {
+            const T r = rcp(L(i, i));
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                B(i, c0 + c) = w[c] * r;
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        T w[NB];
+        const T r = rcp(L(i, i));
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            w[c] = UNIT ? B(i, c0 + c) * r : B(i, c0 + c);
+        for (int l = i + 1; l < n; ++l) {
+            const T a = L(l, i);
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                w[c] = fma(-a, B(l, c0 + c), w[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            B(i, c0 + c) = UNIT ? w[c] : w[c] * r;
+    }
+}
+
+template <typename T, bool UNIT> __device__ void sym_solve_lane(int n, int nrhs, LV<T> L, LV<T> B)
+{
+    int c0 = 0;
+    for (; c0 + 4 <= nrhs; c0 += 4)
+        sym_solve_block<T, UNIT, 4>(n, L, B, c0);
+    if (nrhs - c0 >= 2) {
+        sym_solve_block<T, UNIT, 2>(n, L, B, c0);
+        c0 += 2;
+    }
+    if (nrhs - c0 >= 1) sym_solve_block<T, UNIT, 1>(n, L, B, c0);
+}
+
+// ---------------------------------------------------------------------
+// Triangular solve, any side / uplo / trans / diag, through views
+// (src/cbk_trsm_compact.hpp:73-228)
+// ---------------------------------------------------------------------
+
+// op(A) X = alpha B for the NB columns c0 .. c0+NB-1 of B, row by row
+// (the reference's row-dot form, src/cbk_trsm_compact.hpp:73-104).
+template <typename T, int NB>
+__device__ void trsm_left_block(bool back, bool tran, bool unit, int m, T alpha, LV<T> A, LV<T> B,
+                                int c0)
+{
+    for (int t = 0; t < m; ++t) {
+        const int i = back ? m - 1 - t : t;
+        T w[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            w[c] = B(i, c0 + c) * alpha;
+        const int lo = back ? i + 1 : 0, hi = back ? m : i;
+        for (int l = lo; l < hi; ++l) {
+            const T a = tran ? A(l, i) : A(i, l);
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                w[c] = fma(-a, B(l, c0 + c), w[c]);
+        }
+        if (unit) {
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                B(i, c0 + c) = w[c];
+        }
+        else {
+            const T r = rcp(A(i, i));
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                B(i, c0 + c) = w[c] * r;
+        }
+    }
+}
+
+template <typename T>
+__device__ void trsm_lane(bool left, bool upper, bool tran, bool unit, int m, int n, T alpha,
+                          LV<T> A, LV<T> B)
+{
+    if (left) {
+        const bool back = (upper != tran);
+        int c0 = 0;
+        for (; c0 + 4 <= n; c0 += 4)
+            trsm_left_block<T, 4>(back, tran, unit, m, alpha, A, B, c0);
+        if (n - c0 >= 2) {
+            trsm_left_block<T, 2>(back, tran, unit, m, alpha, A, B, c0);
+            c0 += 2;
+        }
+        if (n - c0 >= 1) trsm_left_block<T, 1>(back, tran, unit, m, alpha, A, B, c0);
+    }
+    else {
+        // X op(A) = alpha B, X column by column (the reference's side-R form,
+        // src/cbk_trsm_compact.hpp:206-227)
+        const bool fwd = (upper != tran);
+        for (int t = 0; t < n; ++t) {
+            const int j = fwd ? t : n - 1 - t;
+            for (int i = 0; i < m; ++i)
+                B(i, j) = B(i, j) * alpha;
+            const int lo = fwd ? 0 : j + 1, hi = fwd ? j : n;
+            for (int l = lo; l < hi; ++l) {
+                const T c = tran ? A(j, l) : A(l, j);
+                for (int i = 0; i < m; ++i)
+                    B(i, j) = fma(-c, B(i, l), B(i, j));
+            }
+            if (!unit) {
+                const T r = rcp(A(j, j));
+                for (int i = 0; i < m; ++i)
+                    B(i, j) = B(i, j) * r;
+            }
+        }
+    }
+}
+
+template <typename T> __device__ void zero_lane(LV<T> B, int i0, int i1, int ncols)
+{
+    for (int j = 0; j < ncols; ++j)
+        for (int i = i0; i < i1; ++i)
+            B(i, j) = T(0);
+}
+
+// ---------------------------------------------------------------------
+// Householder QR family (src/cbk_geqrf_compact.hpp:74-131,
+// src/cbk_ormqr_compact.hpp:68-124, src/cbk_orgqr_compact.hpp:50-87)
+// ---------------------------------------------------------------------
+
+// H(kk) = I - t v v^T applied to the NB slices c0 .. c0+NB-1 of C,
+// v = (1, A(kk+1:len, kk)): w = v^T c, w *= t, c -= v w
+// (larf_block, src/cbk_ormqr_compact.hpp:68-91).
+template <typename T, int NB>
+__device__ void larf_block(int kk, int len, LV<T> A, T t, LV<T> C, int c0)
+{
+    T w[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c)
+        w[c] = C(kk, c0 + c);
+    for (int i = kk + 1; i < len; ++i) {
+        const T a = A(i, kk);
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            w[c] = fma(a, C(i, c0 + c), w[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        w[c] *= t;
+        C(kk, c0 + c) -= w[c];
+    }
+    for (int i = kk + 1; i < len; ++i) {
+        const T a = A(i, kk);
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+            C(i, c0 + c) = fma(-a, w[c], C(i, c0 + c));
+    }
+}
+
+template <typename T>
+__device__ void larf_lane(int kk, int len, LV<T> A, T t, LV<T> C, int p0, int p1)
+{
+    int c0 = p0;
+    for (; c0 + 4 <= p1; c0 += 4)
+        larf_block<T, 4>(kk, len, A, t, C, c0);
+    if (p1 - c0 >= 2) {
+        larf_block<T, 2>(kk, len, A, t, C, c0);
+        c0 += 2;
+    }
+    if (p1 - c0 >= 1) larf_block<T, 1>(kk, len, A, t, C, c0);
+}
+
+// geqr2 on the lane view: per column the tail sum of squares, the branch-free
+// larfg (no reflector when the tail is exactly zero), the body scaled by
+// 1/(x0 - beta), then H applied to the trailing columns. tau has stride V.
+template <typename T> __device__ void geqrf_lane(int m, int n, LV<T> A, T *tau, int V)
+{
+    const int k = min(m, n);
+    for (int kk = 0; kk < k; ++kk) {
+        T tail = T(0);
+        for (int i = kk + 1; i < m; ++i) {
+            const T a = A(i, kk);
+            tail = fma(a, a, tail);
+        }
+        const T x0 = A(kk, kk);
+        const T norm = sqrt(fma(x0, x0, tail));
+        const T beta = (x0 >= T(0)) ? -norm : norm;
+        const bool has = tail > T(0);
+        const T t = has ? (beta - x0) / beta : T(0);
+        const T inv = has ? rcp(x0 - beta) : T(0);
+        tau[(long)kk * V] = t;
+        for (int i = kk + 1; i < m; ++i)
+            A(i, kk) = A(i, kk) * inv;
+        A(kk, kk) = has ? beta : x0;
+        larf_lane<T>(kk, m, A, t, A, kk + 1, n);
+    }
+}
+
+template <typename T>
+__device__ void ormqr_lane(bool forward, int len, int npanel, int k, LV<T> A, const T *tau, int V,
+                           LV<T> C)
+{
+    for (int s = 0; s < k; ++s) {
+        const int kk = forward ? s : k - 1 - s;
+        larf_lane<T>(kk, len, A, tau[(long)kk * V], C, 0, npanel);
+    }
+}
+
+template <typename T> __device__ void orgqr_lane(int m, int n, int k, LV<T> A, const T *tau, int V)
+{
+    for (int j = k; j < n; ++j) {
+        for (int i = 0; i < m; ++i)
+            A(i, j) = T(0);
+        A(j, j) = T(1);
+    }
+    for (int kk = k - 1; kk >= 0; --kk) {
+        const T t = tau[(long)kk * V];
+        larf_lane<T>(kk, m, A, t, A, kk + 1, n);
+        const T mt = -t;
+        for (int i = kk + 1; i < m; ++i)
+            A(i, kk) = A(i, kk) * mt;
+        A(kk, kk) = T(1) - t;
+        for (int i = 0; i < kk; ++i)
+            A(i, kk) = T(0);
+    }
+}
+
+// One lane of the least-squares solve (src/cbk_gels_compact.hpp:84-106): F is
+// the tall (p x q) view of A, B its p x nrhs right-hand sides.
+template <typename T>
+__device__ void gels_lane(bool overdet, int p, int q, int nrhs, LV<T> F, T *tau, int V, LV<T> B)
+{
+    geqrf_lane<T>(p, q, F, tau, V);
+    if (overdet) {
+        ormqr_lane<T>(true, p, nrhs, q, F, tau, V, B);
+        trsm_lane<T>(true, true, false, false, q, nrhs, T(1), F, B);
+    }
+    else {
+        trsm_lane<T>(true, true, true, false, q, nrhs, T(1), F, B);
+        zero_lane<T>(B, q, p, nrhs);
+        ormqr_lane<T>(false, p, nrhs, q, F, tau, V, B);
+    }
+}
+
+} // namespace cbkdev

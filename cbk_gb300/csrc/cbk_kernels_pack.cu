@@ -1,0 +1,172 @@
+// cbk_kernels_pack.cu -- device conversion between a dense batch (one matrix
+// after another, LAPACK storage) and the compact layout, the device-side form
+// of the reference tests' pack_compact / unpack_compact
+// (tests/test_compact_util.hpp:477-531): padded lanes of a partial last group
+// receive pad_diag on the diagonal and zero elsewhere.
+//
+// Memory-bound transposes. A block stages a 32-lane x 32-element tile in
+// shared memory: the dense side is read (or written) 32 consecutive elements
+// of one matrix at a time, the compact side 32 consecutive lanes of one
+// element at a time, so both sides are coalesced. Elements are numbered in the
+// dense matrix's own storage order (column-major: e = i + j*m; row-major:
+// e = i*n + j), which keeps the dense side contiguous when lda is the
+// matrix's extent.
+#include "cbk_device.cuh"
+#include "cbk_launch.h"
+
+namespace cbkcuda {
+
+namespace {
+
+constexpr int TILE = 32;
+constexpr int ROWS = 8; // block = TILE x ROWS threads
+
+struct PackGeom {
+    int m, n, lda, ldap, V, nm;
+    long long stride;
+    bool row;
+    long nelem;  // m * n
+    long nlanes; // padded lane count
+    size_t gs;   // scalars per compact group
+};
+
+// Element e -> (i, j) in the dense storage order.
+__device__ __forceinline__ void elem_ij(const PackGeom &G, long e, int &i, int &j)
+{
+    if (G.row) {
+        i = (int)(e / G.n);
+        j = (int)(e - (long)i * G.n);
+    }
+    else {
+        j = (int)(e / G.m);
+        i = (int)(e - (long)j * G.m);
+    }
+}
+
+__device__ __forceinline__ size_t dense_off(const PackGeom &G, long mat, int i, int j)
+{
+    return (size_t)mat * (size_t)G.stride +
+           (G.row ? (size_t)i * G.lda + j : (size_t)j * G.lda + i);
+}
+
+__device__ __forceinline__ size_t compact_off(const PackGeom &G, long lane, int i, int j)
+{
+    const long g = lane / G.V;
+    const int v = (int)(lane - g * G.V);
+    const size_t in = G.row ? (size_t)i * G.ldap + j : (size_t)j * G.ldap + i;
+    return (size_t)g * G.gs + in * (size_t)G.V + v;
+}
+
+// grid: x over lane tiles, y over element tiles
+template <typename T>
+__global__ void k_pack(PackGeom G, const T *__restrict__ a, T *__restrict__ ap, T pad_diag)
+{
+    __shared__ T tile[TILE][TILE + 1];
+    const long e0 = (long)blockIdx.y * TILE;
+    const long l0 = (long)blockIdx.x * TILE;
+    // read: lane l0+r, elements e0 .. e0+31 (consecutive threads, consecutive elements)
+    for (int r = threadIdx.y; r < TILE; r += ROWS) {
+        const long lane = l0 + r;
+        const long e = e0 + threadIdx.x;
+        T x = T(0);
+        if (lane < G.nlanes && e < G.nelem) {
+            int i, j;
+            elem_ij(G, e, i, j);
+            if (lane < G.nm)
+                x = a[dense_off(G, lane, i, j)];
+            else
+                x = (i == j) ? pad_diag : T(0);
+        }
+        tile[r][threadIdx.x] = x;
+    }
+    __syncthreads();
+    // write: element e0+r, lanes l0 .. l0+31 (consecutive threads, consecutive lanes)
+    for (int r = threadIdx.y; r < TILE; r += ROWS) {
+        const long e = e0 + r;
+        const long lane = l0 + threadIdx.x;
+        if (lane < G.nlanes && e < G.nelem) {
+            int i, j;
+            elem_ij(G, e, i, j);
+            ap[compact_off(G, lane, i, j)] = tile[threadIdx.x][r];
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_unpack(PackGeom G, const T *__restrict__ ap, T *__restrict__ a)
+{
+    __shared__ T tile[TILE][TILE + 1];
+    const long e0 = (long)blockIdx.y * TILE;
+    const long l0 = (long)blockIdx.x * TILE;
+    for (int r = threadIdx.y; r < TILE; r += ROWS) {
+        const long e = e0 + r;
+        const long lane = l0 + threadIdx.x;
+        T x = T(0);
+        if (lane < G.nm && e < G.nelem) {
+            int i, j;
+            elem_ij(G, e, i, j);
+            x = ap[compact_off(G, lane, i, j)];
+        }
+        tile[threadIdx.x][r] = x;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < TILE; r += ROWS) {
+        const long lane = l0 + r;
+        const long e = e0 + threadIdx.x;
+        if (lane < G.nm && e < G.nelem) {
+            int i, j;
+            elem_ij(G, e, i, j);
+            a[dense_off(G, lane, i, j)] = tile[r][threadIdx.x];
+        }
+    }
+}
+
+PackGeom make_geom(bool row, int m, int n, int lda, long long stride, int ldap, int V, int nm)
+{
+    PackGeom G;
+    G.m = m;
+    G.n = n;
+    G.lda = lda;
+    G.ldap = ldap;
+    G.V = V;
+    G.nm = nm;
+    G.stride = stride;
+    G.row = row;
+    G.nelem = (long)m * n;
+    G.nlanes = (((long)nm + V - 1) / V) * V;
+    G.gs = cbkdev::gstride(row, ldap, m, n, V);
+    return G;
+}
+
+} // namespace
+
+template <typename T>
+cudaError_t launch_pack(bool row, int m, int n, const T *a, int lda, long long stride, T *ap,
+                        int ldap, int V, int nm, T pad_diag, cudaStream_t s)
+{
+    const PackGeom G = make_geom(row, m, n, lda, stride, ldap, V, nm);
+    const dim3 grid((unsigned)((G.nlanes + TILE - 1) / TILE), (unsigned)((G.nelem + TILE - 1) / TILE));
+    k_pack<T><<<grid, dim3(TILE, ROWS), 0, s>>>(G, a, ap, pad_diag);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_unpack(bool row, int m, int n, const T *ap, int ldap, T *a, int lda,
+                          long long stride, int V, int nm, cudaStream_t s)
+{
+    const PackGeom G = make_geom(row, m, n, lda, stride, ldap, V, nm);
+    const dim3 grid((unsigned)((nm + TILE - 1) / TILE), (unsigned)((G.nelem + TILE - 1) / TILE));
+    k_unpack<T><<<grid, dim3(TILE, ROWS), 0, s>>>(G, ap, a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_pack<float>(bool, int, int, const float *, int, long long, float *, int,
+                                        int, int, float, cudaStream_t);
+template cudaError_t launch_pack<double>(bool, int, int, const double *, int, long long, double *,
+                                         int, int, int, double, cudaStream_t);
+template cudaError_t launch_unpack<float>(bool, int, int, const float *, int, float *, int,
+                                          long long, int, int, cudaStream_t);
+template cudaError_t launch_unpack<double>(bool, int, int, const double *, int, double *, int,
+                                           long long, int, int, cudaStream_t);
+
+} // namespace cbkcuda

@@ -1,0 +1,373 @@
+// cbk_kernels_refine.cu -- mixed-precision SPD solve: FP32 Cholesky, FP64
+// iterative refinement, per-matrix FP64 fallback.
+//
+// No counterpart in the reference (whose solves are FP64 or FP32 throughout,
+// src/cbk_posv_compact.hpp); the method is LAPACK dsposv's, per lane of the
+// compact batch:
+//   1. A (FP64, the lower triangle of the view) is rounded to FP32 -- a lane
+//      whose entries overflow FP32 falls back (iters = -2) -- and factored in
+//      FP32 -- a lane with a non-positive FP32 pivot falls back (iters = -1);
+//   2. per right-hand side: x = solve32(b); then repeat r = b - A x in FP64,
+//      stop when ||r||_inf <= sqrt(n) eps64 ||A||_inf ||x||_inf (dsposv's
+//      test), else x += solve32(fl32(r)); a lane falls back (iters = -3) when
+//      max_iter corrections did not converge or a correction failed to halve
+//      the residual (refinement stalled);
+//   3. a lane that falls back runs the plain FP64 path's factor and solve on
+//      its own A and on the right-hand sides not yet solved: A then holds the
+//      FP64 factor (as dsposv leaves it); a converged lane leaves A untouched.
+// iters[idx] = corrections used (max over the right-hand sides), or the
+// negative fallback code; berr[idx] = the largest normwise backward error
+// ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) of the lane's solutions,
+// from the FP64 residual of the accepted x (NaN for a lane that fell back).
+//
+// On a GB300 the FP64 pipe runs at ~1/58 of the FP32 rate, so the FP64 work
+// per right-hand side falls from n^3/6 + n^2 fused multiply-adds and 2n long
+// operations to n^2 per refinement step.
+//
+// Two variants: orders up to 16 keep the FP32 factor and x in registers
+// (compile-time order); larger orders keep the FP32 factor, x and the
+// correction in the caller's workspace, in the compact layout (coalesced),
+// sized by cbk_cuda_dposv_refined_compact_lwork.
+#include "cbk_device.cuh"
+#include "cbk_launch.h"
+
+#include <float.h>
+#include <math.h>
+
+namespace cbkcuda {
+using namespace cbkdev;
+
+namespace {
+
+constexpr double EPS64 = 2.220446049250313e-16;
+constexpr int REG_NMAX = 16;
+
+// packed lower-triangle index (column-major), i >= j
+__host__ __device__ constexpr int tix(int i, int j, int N)
+{
+    return j * (2 * N - j + 1) / 2 + (i - j);
+}
+
+__device__ __forceinline__ bool fits_fp32(double a)
+{
+    return !(fabs(a) > (double)FLT_MAX); // NaN passes: garbage in, garbage out
+}
+
+struct RefineOut {
+    int *iters;
+    double *berr;
+    int nm;
+    int max_iter;
+};
+
+// The FP64 fallback of one lane: factor A in place (the plain path's
+// arithmetic) and solve columns first .. nrhs-1 of B. Not inlined: the rare
+// path keeps its registers out of the refinement loop's budget.
+__device__ __noinline__ void fallback_lane(int n, int nrhs, int first, LV<double> A, LV<double> B)
+{
+    factor_lane<double, false>(n, A);
+    if (first < nrhs) {
+        LV<double> Bs = B;
+        Bs.p += (long)first * B.sj;
+        sym_solve_lane<double, false>(n, nrhs - first, A, Bs);
+    }
+}
+
+__device__ __forceinline__ void write_status(const RefineOut &o, long idx, int status, int it,
+                                             double berr)
+{
+    if (idx >= o.nm) return; // padded lanes compute but report nothing
+    if (o.iters) o.iters[idx] = status != 0 ? status : it;
+    if (o.berr) o.berr[idx] = status != 0 ? (double)NAN : berr;
+}
+
+// ---------------------------------------------------------------------
+// registers: compile-time order N <= 16
+// ---------------------------------------------------------------------
+
+// z := (L L^T)^-1 z in FP32, L packed lower with reciprocal pivots rinv
+template <int N>
+__device__ __forceinline__ void solve32(const float (&L)[N * (N + 1) / 2], const float (&rinv)[N],
+                                        float (&z)[N])
+{
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float w = z[i];
+#pragma unroll
+        for (int l = 0; l < i; ++l)
+            w = fmaf(-L[tix(i, l, N)], z[l], w);
+        z[i] = w * rinv[i];
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; --i) {
+        float w = z[i];
+#pragma unroll
+        for (int l = i + 1; l < N; ++l)
+            w = fmaf(-L[tix(l, i, N)], z[l], w);
+        z[i] = w * rinv[i];
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128)
+    k_posv_refined_reg(bool row, bool up, int nrhs, double *ap, int ldap, double *bp, int ldbp,
+                       int V, long ngroups, size_t sa, size_t sb, RefineOut out)
+{
+    Lane ln;
+    if (!lane_of(ngroups, V, ln)) return;
+    const long idx = ln.g * V + ln.v;
+    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V);
+    if (up) A = A.t();
+    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
+
+    float L[N * (N + 1) / 2];
+    float rs[N];
+    int status = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        rs[i] = 0.f;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+        for (int i = j; i < N; ++i) {
+            const double a = A(i, j);
+            if (!fits_fp32(a)) status = -2;
+            const float f = (float)a;
+            L[tix(i, j, N)] = f;
+            rs[i] += fabsf(f);
+            if (i != j) rs[j] += fabsf(f);
+        }
+    float anorm = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        anorm = fmaxf(anorm, rs[i]);
+    float rinv[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        const float a = L[tix(j, j, N)];
+        if (!(a > 0.f) && status == 0) status = -1;
+        const float d = sqrtf(a);
+        const float r = 1.0f / d;
+        rinv[j] = r;
+        L[tix(j, j, N)] = d;
+#pragma unroll
+        for (int i = j + 1; i < N; ++i)
+            L[tix(i, j, N)] *= r;
+#pragma unroll
+        for (int c = j + 1; c < N; ++c)
+#pragma unroll
+            for (int i = c; i < N; ++i)
+                L[tix(i, c, N)] = fmaf(-L[tix(i, j, N)], L[tix(c, j, N)], L[tix(i, c, N)]);
+    }
+    const double cte = (double)anorm * EPS64 * sqrt((double)N);
+    int it_max = 0, col = 0;
+    double worst = 0.0;
+    for (; col < nrhs && status == 0; ++col) {
+        double x[N];
+        float z[N];
+        double bnorm = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const double b = B(i, col);
+            bnorm = fmax(bnorm, fabs(b));
+            z[i] = (float)b;
+        }
+        solve32<N>(L, rinv, z);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            x[i] = (double)z[i];
+        double rprev = INFINITY;
+        for (int it = 0;; ++it) {
+            // opaque strides: the n^2 addresses of A are recomputed each step
+            // (cheap integer work) instead of being hoisted into registers
+            LV<double> Ar = A;
+            asm volatile("" : "+l"(Ar.si), "+l"(Ar.sj));
+            double rnorm = 0.0, xnorm = 0.0;
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                double acc = B(i, col);
+#pragma unroll
+                for (int j = 0; j < N; ++j)
+                    acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
+                rnorm = fmax(rnorm, fabs(acc));
+                xnorm = fmax(xnorm, fabs(x[i]));
+                z[i] = (float)acc;
+            }
+            if (rnorm <= cte * xnorm) {
+                const double den = (double)anorm * xnorm + bnorm;
+                worst = fmax(worst, den > 0.0 ? rnorm / den : 0.0);
+                it_max = max(it_max, it);
+                break;
+            }
+            if (it >= out.max_iter || !(rnorm <= 0.5 * rprev)) {
+                status = -3;
+                break;
+            }
+            rprev = rnorm;
+            solve32<N>(L, rinv, z);
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                x[i] += (double)z[i];
+        }
+        if (status == 0) {
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                B(i, col) = x[i];
+        }
+    }
+    if (status != 0) fallback_lane(N, nrhs, status == -3 ? col - 1 : 0, A, B);
+    write_status(out, idx, status, it_max, worst);
+}
+
+// ---------------------------------------------------------------------
+// workspace: any order
+// ---------------------------------------------------------------------
+
+struct RefineWork {
+    float *L;   // n x n FP32 factor per lane, compact, ld = n
+    double *x;  // n per lane
+    float *z;   // n per lane
+};
+
+__global__ void __launch_bounds__(128)
+    k_posv_refined_ws(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
+                      int ldbp, int V, long ngroups, size_t sa, size_t sb, RefineWork w,
+                      RefineOut out)
+{
+    Lane ln;
+    if (!lane_of(ngroups, V, ln)) return;
+    const long idx = ln.g * V + ln.v;
+    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V);
+    if (up) A = A.t();
+    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
+    const LV<float> W = lv_make<float>(w.L + ln.g * ((size_t)n * n * V) + ln.v, false, n, V);
+    double *X = w.x + ln.g * ((size_t)n * V) + ln.v;
+    float *Z = w.z + ln.g * ((size_t)n * V) + ln.v;
+    const LV<float> Zv{Z, (long)V, 0};
+
+    int status = 0;
+    for (int j = 0; j < n; ++j)
+        for (int i = j; i < n; ++i) {
+            const double a = A(i, j);
+            if (!fits_fp32(a)) status = -2;
+            W(i, j) = (float)a;
+        }
+    float anorm = 0.f;
+    for (int i = 0; i < n; ++i) {
+        float s = 0.f;
+        for (int j = 0; j <= i; ++j)
+            s += fabsf(W(i, j));
+        for (int j = i + 1; j < n; ++j)
+            s += fabsf(W(j, i));
+        anorm = fmaxf(anorm, s);
+    }
+    if (status == 0) {
+        factor_lane<float, false>(n, W);
+        for (int i = 0; i < n; ++i)
+            if (!(W(i, i) > 0.f)) status = -1;
+    }
+    const double cte = (double)anorm * EPS64 * sqrt((double)n);
+    int it_max = 0, col = 0;
+    double worst = 0.0;
+    for (; col < nrhs && status == 0; ++col) {
+        double bnorm = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double b = B(i, col);
+            bnorm = fmax(bnorm, fabs(b));
+            Z[(long)i * V] = (float)b;
+        }
+        sym_solve_block<float, false, 1>(n, W, Zv, 0);
+        for (int i = 0; i < n; ++i)
+            X[(long)i * V] = (double)Z[(long)i * V];
+        double rprev = INFINITY;
+        for (int it = 0;; ++it) {
+            double rnorm = 0.0, xnorm = 0.0;
+            for (int i = 0; i < n; ++i) {
+                double acc = B(i, col);
+                for (int j = 0; j <= i; ++j)
+                    acc = fma(-A(i, j), X[(long)j * V], acc);
+                for (int j = i + 1; j < n; ++j)
+                    acc = fma(-A(j, i), X[(long)j * V], acc);
+                rnorm = fmax(rnorm, fabs(acc));
+                xnorm = fmax(xnorm, fabs(X[(long)i * V]));
+                Z[(long)i * V] = (float)acc;
+            }
+            if (rnorm <= cte * xnorm) {
+                const double den = (double)anorm * xnorm + bnorm;
+                worst = fmax(worst, den > 0.0 ? rnorm / den : 0.0);
+                it_max = max(it_max, it);
+                break;
+            }
+            if (it >= out.max_iter || !(rnorm <= 0.5 * rprev)) {
+                status = -3;
+                break;
+            }
+            rprev = rnorm;
+            sym_solve_block<float, false, 1>(n, W, Zv, 0);
+            for (int i = 0; i < n; ++i)
+                X[(long)i * V] += (double)Z[(long)i * V];
+        }
+        if (status == 0)
+            for (int i = 0; i < n; ++i)
+                B(i, col) = X[(long)i * V];
+    }
+    if (status != 0) fallback_lane(n, nrhs, status == -3 ? col - 1 : 0, A, B);
+    write_status(out, idx, status, it_max, worst);
+}
+
+inline size_t align256(size_t b)
+{
+    return (b + 255) & ~(size_t)255;
+}
+
+} // namespace
+
+// bytes of workspace the refined solve needs (0 when it runs from registers)
+size_t posv_refined_lwork(int n, int nrhs, int V, int nm)
+{
+    (void)nrhs;
+    if (n <= REG_NMAX || nm <= 0) return 0;
+    const size_t lanes = (size_t)((nm + V - 1) / V) * V;
+    return align256(lanes * (size_t)n * n * sizeof(float)) +
+           align256(lanes * (size_t)n * sizeof(double)) + align256(lanes * (size_t)n * sizeof(float));
+}
+
+cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
+                                double *berr, void *work, cudaStream_t s)
+{
+    const long ng = ((long)nm + V - 1) / V;
+    const size_t sa = gstride(row, ldap, n, n, V), sb = gstride(row, ldbp, n, nrhs, V);
+    const RefineOut out{iters, berr, nm, max_iter};
+    const int th = 128;
+    const unsigned bl = (unsigned)((ng * V + th - 1) / th);
+    if (n <= REG_NMAX) {
+        switch (n) {
+#define CBK_REG_CASE(N)                                                                            \
+    case N:                                                                                        \
+        k_posv_refined_reg<N><<<bl, th, 0, s>>>(row, up, nrhs, ap, ldap, bp, ldbp, V, ng, sa, sb,  \
+                                                out);                                              \
+        break;
+            CBK_REG_CASE(1) CBK_REG_CASE(2) CBK_REG_CASE(3) CBK_REG_CASE(4) CBK_REG_CASE(5)
+            CBK_REG_CASE(6) CBK_REG_CASE(7) CBK_REG_CASE(8) CBK_REG_CASE(9) CBK_REG_CASE(10)
+            CBK_REG_CASE(11) CBK_REG_CASE(12) CBK_REG_CASE(13) CBK_REG_CASE(14) CBK_REG_CASE(15)
+            CBK_REG_CASE(16)
+#undef CBK_REG_CASE
+        default: break;
+        }
+        return cudaGetLastError();
+    }
+    const size_t lanes = (size_t)ng * V;
+    char *base = static_cast<char *>(work);
+    RefineWork w;
+    w.L = reinterpret_cast<float *>(base);
+    base += align256(lanes * (size_t)n * n * sizeof(float));
+    w.x = reinterpret_cast<double *>(base);
+    base += align256(lanes * (size_t)n * sizeof(double));
+    w.z = reinterpret_cast<float *>(base);
+    k_posv_refined_ws<<<bl, th, 0, s>>>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, ng, sa, sb, w,
+                                        out);
+    return cudaGetLastError();
+}
+
+} // namespace cbkcuda

@@ -1,0 +1,74 @@
+// cbk_launch.h -- internal interface between the C-ABI layer (cbk_api.cpp)
+// and the CUDA kernels. Not installed; include/cbk_cuda.h is the public ABI.
+//
+// Every launcher enqueues its kernel(s) on `stream` and returns the CUDA
+// error of the launch (cudaSuccess when it was queued). Arguments are already
+// validated by the caller; nm >= 1 and every extent the kernel reads is >= 1.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace cbkcuda {
+
+// Threads per block of the lane-per-matrix kernels (the autotuner may change
+// it per routine and order; 0 selects the built-in default).
+int threads_for(int routine, int n, int dsize);
+
+enum Routine {
+    R_POTRF = 0, R_SYTRFNP, R_POTRS, R_POSV, R_SYTRSNP, R_SYSVNP, R_TRSM, R_GEQRF, R_ORMQR,
+    R_ORGQR, R_GELS, R_ZERO, R_PACK, R_UNPACK, R_POSV_REFINED, R_GELS_REFINED, R_SYSVNP_BUCKETED,
+    R_COUNT
+};
+
+// every group of a rows x cols batch := 0
+template <typename T>
+cudaError_t launch_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, int nm,
+                        cudaStream_t s);
+
+// potrf (ldlt = false) / sytrfnp (ldlt = true) of the named triangle
+template <typename T>
+cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, int V, int nm,
+                          cudaStream_t s);
+
+// potrs / posv (ldlt = false), sytrsnp / sysvnp (ldlt = true); fused = factor first
+template <typename T>
+cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, int nrhs, T *ap,
+                             int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_trsm(bool left, bool up, bool row, bool tran, bool unit, int m, int n, T alpha,
+                        const T *ap, int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_geqrf(bool row, int m, int n, T *ap, int ldap, T *taup, int V, int nm,
+                         cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_ormqr(bool left, bool row, bool tran, int m, int n, int k, const T *ap,
+                         int ldap, const T *taup, T *cp, int ldcp, int V, int nm, cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_orgqr(bool row, int m, int n, int k, T *ap, int ldap, const T *taup, int V,
+                         int nm, cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_gels(bool row, bool tran, int m, int n, int nrhs, T *ap, int ldap, T *bp,
+                        int ldbp, T *taup, int V, int nm, cudaStream_t s);
+
+// dense batch (matrix idx at a + idx*stride, element (i,j) at i + j*lda
+// column-major or i*lda + j row-major) <-> compact; padded lanes get pad_diag
+template <typename T>
+cudaError_t launch_pack(bool row, int m, int n, const T *a, int lda, long long stride, T *ap,
+                        int ldap, int V, int nm, T pad_diag, cudaStream_t s);
+template <typename T>
+cudaError_t launch_unpack(bool row, int m, int n, const T *ap, int ldap, T *a, int lda,
+                          long long stride, int V, int nm, cudaStream_t s);
+
+// mixed-precision SPD solve (cbk_kernels_refine.cu)
+size_t posv_refined_lwork(int n, int nrhs, int V, int nm);
+cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
+                                double *berr, void *work, cudaStream_t s);
+
+} // namespace cbkcuda

@@ -1,0 +1,262 @@
+#ifndef CBK_CUDA_H
+#define CBK_CUDA_H
+
+/* cbk_cuda.h -- the compact batch kernels on an NVIDIA GB300 (sm_103a): the
+ * C ABI of libcbk_cuda.so.
+ *
+ * A drop-in for ivan-pi/cbk v0.2.0's include/cbk.h: every routine there has a
+ * counterpart here with the same argument list, the same meaning of each
+ * argument, the same LAPACK-style checks returning -j for an illegal j-th
+ * argument (checked in argument order, before any device work), the same
+ * quick returns and the same in-place results -- with three differences:
+ *
+ *  1. The array arguments are DEVICE pointers (cudaMalloc'd or managed
+ *     memory, or device views of host-registered memory).
+ *  2. Work is enqueued on a CUDA stream: the plain name uses the legacy
+ *     default stream (stream 0), the _async variant takes the stream. Like
+ *     cuBLAS, calls return once the work is queued; the results are ready
+ *     when the stream is synchronised. A CUDA error at launch is returned as
+ *     CBK_CUDA_ERROR_BASE + the cudaError_t code (always > 0).
+ *  3. The interleave width V may also be any multiple of 32 up to 1024 (32
+ *     lanes of a warp then read element (i,j) of 32 matrices as one coalesced
+ *     access); the reference's widths 2, 4, 8 and 16 remain valid.
+ *
+ * Compact layout (include/cbk.h:22-29 of the reference); group g = idx/V,
+ * slot v = idx%V:
+ *   A_v(i,j)  = ap [ g*ldap*ncol*V + (j*ldap + i)*V + v ]   (column-major)
+ *   tau_v(kk) = taup[ g*k*V         +  kk*V          + v ]
+ *   B_v(i,j)  = bp [ g*ldbp*nrhs*V  + (j*ldbp + i)*V + v ]
+ * Row-major swaps the in-matrix index roles (i*ld + j). Every lane of every
+ * group is computed, the padded lanes of a partial last group included, as
+ * the reference does: pack them with the identity (tau with zero).
+ *
+ * The routines never abort and never allocate: the caller owns every buffer.
+ * Numerical failure (a non-SPD lane, a zero pivot, a rank-deficient R) gives
+ * Inf/NaN confined to that lane, as in the reference.
+ */
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CBK_CUDA_VERSION_MAJOR 0
+#define CBK_CUDA_VERSION_MINOR 2
+#define CBK_CUDA_VERSION_PATCH 0
+#define CBK_CUDA_VERSION                                                                 \
+    (CBK_CUDA_VERSION_MAJOR * 10000 + CBK_CUDA_VERSION_MINOR * 100 + CBK_CUDA_VERSION_PATCH)
+
+/* A CUDA launch failure is reported as this base plus the cudaError_t. */
+#define CBK_CUDA_ERROR_BASE 1000
+
+/* Same type as cudaStream_t; 0 is the legacy default stream. */
+typedef struct CUstream_st *cbk_stream_t;
+
+/* Replaces cbk_get_version (include/cbk.h:77, src/cbk.cpp:36-39): the version
+ * of the API implemented, encoded as CBK_VERSION is (0.2.0 -> 200). */
+int cbk_cuda_get_version(void);
+
+/* 1 if V is an accepted interleave width (2, 4, 8, 16, or 32*k <= 1024). */
+int cbk_cuda_vlen_ok(int V);
+
+/* A short description of a return code (0, -j, or a CUDA error). */
+const char *cbk_cuda_status_string(int info);
+
+/* The declarations below come in pairs per scalar type (d = double,
+ * s = float): NAME(...) on stream 0 and NAME_async(..., stream). */
+
+/* QR factorization (include/cbk.h:96-113). -1 layout -2 m -3 n -5 ldap -7 V -8 nm */
+int cbk_cuda_dgeqrf_compact(char layout, int m, int n, double *ap, int ldap, double *taup,
+                            int V, int nm);
+int cbk_cuda_dgeqrf_compact_async(char layout, int m, int n, double *ap, int ldap,
+                                  double *taup, int V, int nm, cbk_stream_t stream);
+int cbk_cuda_sgeqrf_compact(char layout, int m, int n, float *ap, int ldap, float *taup,
+                            int V, int nm);
+int cbk_cuda_sgeqrf_compact_async(char layout, int m, int n, float *ap, int ldap, float *taup,
+                                  int V, int nm, cbk_stream_t stream);
+
+/* Apply Q or Q^T from either side (include/cbk.h:115-143).
+ * -1 layout -2 side -3 trans -4 m -5 n -6 k -8 ldap -11 ldcp -12 V -13 nm */
+int cbk_cuda_dormqr_compact(char layout, char side, char trans, int m, int n, int k,
+                            const double *ap, int ldap, const double *taup, double *cp,
+                            int ldcp, int V, int nm);
+int cbk_cuda_dormqr_compact_async(char layout, char side, char trans, int m, int n, int k,
+                                  const double *ap, int ldap, const double *taup, double *cp,
+                                  int ldcp, int V, int nm, cbk_stream_t stream);
+int cbk_cuda_sormqr_compact(char layout, char side, char trans, int m, int n, int k,
+                            const float *ap, int ldap, const float *taup, float *cp, int ldcp,
+                            int V, int nm);
+int cbk_cuda_sormqr_compact_async(char layout, char side, char trans, int m, int n, int k,
+                                  const float *ap, int ldap, const float *taup, float *cp,
+                                  int ldcp, int V, int nm, cbk_stream_t stream);
+
+/* Form the explicit Q in place (include/cbk.h:145-168).
+ * -1 layout -2 m -3 n -4 k -6 ldap -8 V -9 nm; k = 0 writes I(:, 0:n-1) */
+int cbk_cuda_dorgqr_compact(char layout, int m, int n, int k, double *ap, int ldap,
+                            const double *taup, int V, int nm);
+int cbk_cuda_dorgqr_compact_async(char layout, int m, int n, int k, double *ap, int ldap,
+                                  const double *taup, int V, int nm, cbk_stream_t stream);
+int cbk_cuda_sorgqr_compact(char layout, int m, int n, int k, float *ap, int ldap,
+                            const float *taup, int V, int nm);
+int cbk_cuda_sorgqr_compact_async(char layout, int m, int n, int k, float *ap, int ldap,
+                                  const float *taup, int V, int nm, cbk_stream_t stream);
+
+/* Cholesky factorization (include/cbk.h:170-189). -1 layout -2 uplo -3 n
+ * -5 ldap -6 V -7 nm; the strictly-opposite triangle is never touched */
+int cbk_cuda_dpotrf_compact(char layout, char uplo, int n, double *ap, int ldap, int V,
+                            int nm);
+int cbk_cuda_dpotrf_compact_async(char layout, char uplo, int n, double *ap, int ldap, int V,
+                                  int nm, cbk_stream_t stream);
+int cbk_cuda_spotrf_compact(char layout, char uplo, int n, float *ap, int ldap, int V, int nm);
+int cbk_cuda_spotrf_compact_async(char layout, char uplo, int n, float *ap, int ldap, int V,
+                                  int nm, cbk_stream_t stream);
+
+/* Solve from a Cholesky factor (include/cbk.h:191-216). -1 layout -2 uplo -3 n
+ * -4 nrhs -6 ldap -8 ldbp -9 V -10 nm */
+int cbk_cuda_dpotrs_compact(char layout, char uplo, int n, int nrhs, const double *ap,
+                            int ldap, double *bp, int ldbp, int V, int nm);
+int cbk_cuda_dpotrs_compact_async(char layout, char uplo, int n, int nrhs, const double *ap,
+                                  int ldap, double *bp, int ldbp, int V, int nm,
+                                  cbk_stream_t stream);
+int cbk_cuda_spotrs_compact(char layout, char uplo, int n, int nrhs, const float *ap, int ldap,
+                            float *bp, int ldbp, int V, int nm);
+int cbk_cuda_spotrs_compact_async(char layout, char uplo, int n, int nrhs, const float *ap,
+                                  int ldap, float *bp, int ldbp, int V, int nm,
+                                  cbk_stream_t stream);
+
+/* Fused Cholesky factor + solve (include/cbk.h:218-234): bit-identical to
+ * ?potrf then ?potrs; nrhs = 0 still factors. Codes as ?potrs. */
+int cbk_cuda_dposv_compact(char layout, char uplo, int n, int nrhs, double *ap, int ldap,
+                           double *bp, int ldbp, int V, int nm);
+int cbk_cuda_dposv_compact_async(char layout, char uplo, int n, int nrhs, double *ap, int ldap,
+                                 double *bp, int ldbp, int V, int nm, cbk_stream_t stream);
+int cbk_cuda_sposv_compact(char layout, char uplo, int n, int nrhs, float *ap, int ldap,
+                           float *bp, int ldbp, int V, int nm);
+int cbk_cuda_sposv_compact_async(char layout, char uplo, int n, int nrhs, float *ap, int ldap,
+                                 float *bp, int ldbp, int V, int nm, cbk_stream_t stream);
+
+/* Unpivoted LDL^T factorization (include/cbk.h:236-258). Codes as ?potrf. */
+int cbk_cuda_dsytrfnp_compact(char layout, char uplo, int n, double *ap, int ldap, int V,
+                              int nm);
+int cbk_cuda_dsytrfnp_compact_async(char layout, char uplo, int n, double *ap, int ldap, int V,
+                                    int nm, cbk_stream_t stream);
+int cbk_cuda_ssytrfnp_compact(char layout, char uplo, int n, float *ap, int ldap, int V,
+                              int nm);
+int cbk_cuda_ssytrfnp_compact_async(char layout, char uplo, int n, float *ap, int ldap, int V,
+                                    int nm, cbk_stream_t stream);
+
+/* Solve from an LDL^T factor (include/cbk.h:260-285). Codes as ?potrs. */
+int cbk_cuda_dsytrsnp_compact(char layout, char uplo, int n, int nrhs, const double *ap,
+                              int ldap, double *bp, int ldbp, int V, int nm);
+int cbk_cuda_dsytrsnp_compact_async(char layout, char uplo, int n, int nrhs, const double *ap,
+                                    int ldap, double *bp, int ldbp, int V, int nm,
+                                    cbk_stream_t stream);
+int cbk_cuda_ssytrsnp_compact(char layout, char uplo, int n, int nrhs, const float *ap,
+                              int ldap, float *bp, int ldbp, int V, int nm);
+int cbk_cuda_ssytrsnp_compact_async(char layout, char uplo, int n, int nrhs, const float *ap,
+                                    int ldap, float *bp, int ldbp, int V, int nm,
+                                    cbk_stream_t stream);
+
+/* Fused LDL^T factor + solve (include/cbk.h:287-303). Codes as ?potrs. */
+int cbk_cuda_dsysvnp_compact(char layout, char uplo, int n, int nrhs, double *ap, int ldap,
+                             double *bp, int ldbp, int V, int nm);
+int cbk_cuda_dsysvnp_compact_async(char layout, char uplo, int n, int nrhs, double *ap,
+                                   int ldap, double *bp, int ldbp, int V, int nm,
+                                   cbk_stream_t stream);
+int cbk_cuda_ssysvnp_compact(char layout, char uplo, int n, int nrhs, float *ap, int ldap,
+                             float *bp, int ldbp, int V, int nm);
+int cbk_cuda_ssysvnp_compact_async(char layout, char uplo, int n, int nrhs, float *ap,
+                                   int ldap, float *bp, int ldbp, int V, int nm,
+                                   cbk_stream_t stream);
+
+/* Triangular solve (include/cbk.h:305-333). -1 layout -2 side -3 uplo
+ * -4 transa -5 diag -6 m -7 n -10 ldap -12 ldbp -13 V -14 nm;
+ * alpha = 0 sets B := 0 without reading A */
+int cbk_cuda_dtrsm_compact(char layout, char side, char uplo, char transa, char diag, int m,
+                           int n, double alpha, const double *ap, int ldap, double *bp,
+                           int ldbp, int V, int nm);
+int cbk_cuda_dtrsm_compact_async(char layout, char side, char uplo, char transa, char diag,
+                                 int m, int n, double alpha, const double *ap, int ldap,
+                                 double *bp, int ldbp, int V, int nm, cbk_stream_t stream);
+int cbk_cuda_strsm_compact(char layout, char side, char uplo, char transa, char diag, int m,
+                           int n, float alpha, const float *ap, int ldap, float *bp, int ldbp,
+                           int V, int nm);
+int cbk_cuda_strsm_compact_async(char layout, char side, char uplo, char transa, char diag,
+                                 int m, int n, float alpha, const float *ap, int ldap,
+                                 float *bp, int ldbp, int V, int nm, cbk_stream_t stream);
+
+/* Least squares / minimum norm (include/cbk.h:335-351). -1 layout -2 trans
+ * -3 m -4 n -5 nrhs -7 ldap -9 ldbp -11 V -12 nm; min(m,n) = 0 sets B := 0,
+ * nrhs = 0 does nothing */
+int cbk_cuda_dgels_compact(char layout, char trans, int m, int n, int nrhs, double *ap,
+                           int ldap, double *bp, int ldbp, double *taup, int V, int nm);
+int cbk_cuda_dgels_compact_async(char layout, char trans, int m, int n, int nrhs, double *ap,
+                                 int ldap, double *bp, int ldbp, double *taup, int V, int nm,
+                                 cbk_stream_t stream);
+int cbk_cuda_sgels_compact(char layout, char trans, int m, int n, int nrhs, float *ap,
+                           int ldap, float *bp, int ldbp, float *taup, int V, int nm);
+int cbk_cuda_sgels_compact_async(char layout, char trans, int m, int n, int nrhs, float *ap,
+                                 int ldap, float *bp, int ldbp, float *taup, int V, int nm,
+                                 cbk_stream_t stream);
+
+/* Dense batch <-> compact layout on the device. No reference entry point:
+ * the device form of the reference tests' pack_compact / unpack_compact
+ * (tests/test_compact_util.hpp:477-531) and of mkl_?gepack_compact.
+ * a holds nm m x n matrices, matrix idx at a + idx*stridea, element (i,j) at
+ * i + j*lda (layout 'C') or i*lda + j ('R'); ap is the compact batch in the
+ * same layout. Pack fills the padded lanes of the last group with pad_diag
+ * on the diagonal and zero elsewhere (1 for matrices, 0 for right-hand sides
+ * or tau); unpack writes only the nm real matrices.
+ * pack:   -1 layout -2 m -3 n -5 lda (< max(1, m) 'C' / max(1, n) 'R')
+ *         -6 stridea (< lda * n 'C' / lda * m 'R') -8 ldap -9 V -10 nm
+ * unpack: -1 layout -2 m -3 n -5 ldap -7 lda -8 stridea -9 V -10 nm */
+int cbk_cuda_dpack_compact_async(char layout, int m, int n, const double *a, int lda,
+                                 long long stridea, double *ap, int ldap, int V, int nm,
+                                 double pad_diag, cbk_stream_t stream);
+int cbk_cuda_spack_compact_async(char layout, int m, int n, const float *a, int lda,
+                                 long long stridea, float *ap, int ldap, int V, int nm,
+                                 float pad_diag, cbk_stream_t stream);
+int cbk_cuda_dunpack_compact_async(char layout, int m, int n, const double *ap, int ldap,
+                                   double *a, int lda, long long stridea, int V, int nm,
+                                   cbk_stream_t stream);
+int cbk_cuda_sunpack_compact_async(char layout, int m, int n, const float *ap, int ldap,
+                                   float *a, int lda, long long stridea, int V, int nm,
+                                   cbk_stream_t stream);
+
+/* Mixed-precision SPD solve A X = B: FP32 Cholesky, FP64 iterative refinement
+ * of each right-hand side, FP64 fallback per matrix. No reference entry
+ * point: the ?posv_compact arguments (include/cbk.h:218-234) plus the method
+ * of LAPACK dsposv. Per lane: x = solve32(b); r = b - A x in FP64 until
+ * ||r||_inf <= sqrt(n) eps64 ||A||_inf ||x||_inf, correcting x += solve32(r);
+ * a lane whose FP32 rounding overflows (iters = -2), whose FP32 pivot is not
+ * positive (-1), or whose refinement stalls or exceeds max_iter corrections
+ * (-3) is solved by the FP64 path instead and then holds its FP64 factor in
+ * ap; a converged lane leaves ap unchanged. bp is overwritten with X.
+ *   iters  device int[nm] or NULL: corrections used (max over the lane's
+ *          right-hand sides), or the negative fallback code
+ *   berr   device double[nm] or NULL: the lane's largest normwise backward
+ *          error ||b - A x|| / (||A|| ||x|| + ||b||) (inf-norms), NaN when the
+ *          lane fell back
+ *   work   device workspace of lwork bytes, at least
+ *          cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) (0 for n <= 16,
+ *          where the FP32 factor lives in registers; NULL allowed then)
+ * Returns 0, or -j: -1 layout -2 uplo -3 n -4 nrhs -6 ldap -8 ldbp -9 V
+ * -10 nm -11 max_iter (< 0) -15 lwork (too small). n = 0, nm = 0 or
+ * nrhs = 0 return at once, touching nothing. */
+long long cbk_cuda_dposv_refined_compact_lwork(int n, int nrhs, int V, int nm);
+int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs, double *ap,
+                                         int ldap, double *bp, int ldbp, int V, int nm,
+                                         int max_iter, int *iters, double *berr, void *work,
+                                         long long lwork, cbk_stream_t stream);
+
+/* Calibration, no reference counterpart: the measured fused multiply-add
+ * rate of the current device in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1)
+ * or FP32 (fp64 = 0), from a ~10 ms synthetic kernel -- the denominator of the
+ * FP64-pipe roofline that bounds the FP64 solves on a GB300. Allocates and
+ * synchronises the device; not for use inside a captured stream. */
+int cbk_cuda_measure_fma_rate(int fp64, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CBK_CUDA_H */

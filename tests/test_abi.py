@@ -1,0 +1,98 @@
+"""The C ABI of libcbk_cuda.so on the host (CPU, no GPU needed).
+
+The library must load, export every function include/cbk_cuda.h declares,
+and return the reference's -j argument codes and quick returns before any
+device work: those paths never touch a pointer or the GPU.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import abi_tables
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(cbk_cuda_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_loads():
+    import cbk_gb300
+    lib = cbk_gb300.lib()
+    assert isinstance(lib, ctypes.CDLL)
+    assert cbk_gb300.version() == 200  # the API of the reference's v0.2.0
+
+
+def test_every_declared_symbol_is_exported():
+    import cbk_gb300
+    lib = cbk_gb300.lib()
+    names = declared_functions()
+    assert len(names) >= 50
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_interleave_widths():
+    import cbk_gb300
+    ok = [V for V in range(0, 1100) if cbk_gb300.vlen_ok(V)]
+    assert ok[:4] == [2, 4, 8, 16]
+    assert ok[4:] == list(range(32, 1025, 32))
+
+
+@pytest.mark.parametrize("routine", ["potrf", "sytrfnp", "potrs", "posv", "sytrsnp", "sysvnp",
+                                     "trsm", "geqrf", "ormqr", "orgqr", "gels"])
+def test_argument_checks(routine, oracle_lib):
+    """Every row's code is the expected one, identical in the CUDA library and
+    in the oracle (whose checks are pinned to the reference's)."""
+    import cbk_gb300
+    n = 0
+    for r, dt, args, code in abi_tables.rows_with_codes():
+        if r != routine:
+            continue
+        p = "d" if dt == np.float64 else "s"
+        got = cbk_gb300.call(p, r, *args)
+        assert got == code, (r, dt, args, got, code)
+        assert oracle_lib.call(r, dt, *args) == code, (r, dt, args)
+        n += 1
+    assert n > 20
+
+
+def test_pack_argument_checks():
+    import cbk_gb300
+    N = None
+    # (layout, m, n, a, lda, stridea, ap, ldap, V, nm, pad)
+    b = dict(layout="C", m=4, n=3, a=N, lda=4, stride=12, ap=N, ldap=4, V=32, nm=5, pad=1.0)
+    order = ["layout", "m", "n", "a", "lda", "stride", "ap", "ldap", "V", "nm", "pad"]
+    rows = [(dict(b, layout="X"), -1), (dict(b, m=-1), -2), (dict(b, n=-1), -3),
+            (dict(b, lda=3), -5), (dict(b, stride=11), -6), (dict(b, ldap=3), -8),
+            (dict(b, V=7), -9), (dict(b, nm=-1), -10), (dict(b, nm=0), 0), (dict(b, m=0), 0),
+            (dict(b, layout="R", lda=2, stride=12, ldap=3, nm=0), -5)]
+    for p in "ds":
+        for kw, code in rows:
+            assert cbk_gb300.call(p, "pack", *[kw[k] for k in order]) == code, (kw, code)
+    # unpack: (layout, m, n, ap, ldap, a, lda, stridea, V, nm)
+    u = dict(layout="C", m=4, n=3, ap=N, ldap=4, a=N, lda=4, stride=12, V=32, nm=5)
+    uorder = ["layout", "m", "n", "ap", "ldap", "a", "lda", "stride", "V", "nm"]
+    urows = [(dict(u, layout="X"), -1), (dict(u, ldap=3), -5), (dict(u, lda=3), -7),
+             (dict(u, stride=10), -8), (dict(u, V=33), -9), (dict(u, nm=-2), -10),
+             (dict(u, n=0), 0)]
+    for p in "ds":
+        for kw, code in urows:
+            assert cbk_gb300.call(p, "unpack", *[kw[k] for k in uorder]) == code, (kw, code)
+
+
+def test_status_strings():
+    import cbk_gb300
+    assert cbk_gb300.status_string(0) == "success"
+    assert "illegal" in cbk_gb300.status_string(-3)
+    assert cbk_gb300.status_string(1002)  # a CUDA error text

@@ -1,0 +1,125 @@
+"""The mixed-precision SPD solve (FP32 factor + FP64 refinement) on the GPU.
+
+Workload as the mixed-precision configuration: A = U diag(s) U^T with U
+Haar-random and s log-uniform for condition numbers 1e1 .. 1e6, n in
+{8, 16, 32, 48} (plus orders around the register / workspace boundary).
+Gates, per matrix:
+  * normwise backward error ||b - A x|| / (||A|| ||x|| + ||b||) <= 8 n eps64,
+    computed here in float64 from the original A and B -- the plain FP64
+    path's bound, so both paths meet equal FP64 error;
+  * a converged matrix leaves A bit-for-bit unchanged; a matrix that fell
+    back holds exactly the plain path's FP64 factor;
+  * the reported iters / berr agree with what happened.
+"""
+import numpy as np
+import pytest
+
+import cases as C
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+
+
+def _run(A, B, V=32, layout="C", uplo="L", max_iter=10, nrhs=None):
+    import torch
+
+    import cbk_gb300
+    nm, n, _ = A.shape
+    nrhs = B.shape[2]
+    row = layout == "R"
+    ap = torch.from_numpy(O.pack(A, V, n, row)).cuda()
+    bp = torch.from_numpy(O.pack(B, V, (nrhs if row else n), row, pad_diag=0.0)).cuda()
+    a0 = ap.clone()
+    it = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    be = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+    info = cbk_gb300.dposv_refined_compact(layout, uplo, n, nrhs, ap, n, bp,
+                                           (nrhs if row else n), V, nm, max_iter=max_iter,
+                                           iters=it, berr=be)
+    torch.cuda.synchronize()
+    X = O.unpack(bp.cpu().numpy(), nm, n, nrhs, V, (nrhs if row else n), row)
+    return info, X, ap.cpu().numpy(), a0.cpu().numpy(), it.cpu().numpy(), be.cpu().numpy()
+
+
+def _plain_factor(A, V, layout="C", uplo="L"):
+    import torch
+
+    import cbk_gb300
+    nm, n, _ = A.shape
+    ap = torch.from_numpy(O.pack(A, V, n, layout == "R")).cuda()
+    assert cbk_gb300.dpotrf_compact(layout, uplo, n, ap, n, V, nm) == 0
+    torch.cuda.synchronize()
+    return ap.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 48, 5, 12, 17, 24])
+@pytest.mark.parametrize("layout,uplo", [("C", "L"), ("R", "U")])
+def test_refined_meets_fp64_backward_error(n, layout, uplo, cuda):
+    rng = np.random.default_rng(1000 + n)
+    nm, nrhs, V = 200, 1 if n % 2 == 0 else 2, 32
+    A, kappa = C.gen_spd_cond(rng, nm, n)
+    B = rng.standard_normal((nm, n, nrhs))
+    info, X, a1, a0, it, be = _run(A, B, V, layout, uplo)
+    assert info == 0
+    berr = C.backward_error(A, X, B)
+    assert (berr <= 8 * n * EPS).all(), (berr.max() / (n * EPS), kappa[berr.argmax()])
+    conv = it >= 0
+    fell = ~conv
+    assert set(np.unique(it[fell])) <= {-1, -3}
+    # converged lanes: A untouched, bit for bit
+    row = layout == "R"
+    A0 = O.unpack(a0, nm, n, n, V, n, row)
+    A1 = O.unpack(a1, nm, n, n, V, n, row)
+    assert np.array_equal(A0[conv].view(np.uint64), A1[conv].view(np.uint64))
+    # fallen-back lanes: exactly the plain path's FP64 factor
+    if fell.any():
+        F = O.unpack(_plain_factor(A, V, layout, uplo), nm, n, n, V, n, row)
+        assert np.array_equal(F[fell].view(np.uint64), A1[fell].view(np.uint64))
+    # the kernel's own berr is the FP64 residual's: within rounding of ours
+    assert np.isnan(be[fell]).all()
+    assert (be[conv] <= 8 * n * EPS).all()
+    # well-conditioned matrices converge in few corrections
+    good = kappa < 1e3
+    assert (it[good] >= 0).all() and (it[good] <= 3).all()
+    print(f"n={n}: {conv.mean():.3f} converged, mean corrections {it[conv].mean():.2f}, "
+          f"worst berr {berr.max() / EPS:.2f} eps, fallbacks {np.unique(it[fell])}")
+
+
+def test_refined_fallback_codes(cuda):
+    """-2: an entry overflows FP32; -1: the FP32 factor breaks down
+    (indefinite in FP32, SPD in FP64); -3: max_iter = 0 with an inexact FP32
+    solve. Every such lane still meets the FP64 bound through the fallback."""
+    rng = np.random.default_rng(7)
+    n, nm, V = 8, 64, 32
+    A, _ = C.gen_spd_cond(rng, nm, n, (1.0, 2.0))
+    A[3] *= 1e39                       # overflows FP32
+    A[4] = np.eye(n)
+    A[4, 0, 0] = 1.0 + 1e-12           # exact in FP64; fine in FP32 too
+    Q = C.haar(rng, 1, n)[0]
+    s = np.ones(n)
+    s[-1] = 1e-9                       # SPD in FP64, not positive definite in FP32
+    A[5] = (Q * s) @ Q.T
+    A[5] = np.tril(A[5]) + np.tril(A[5], -1).T
+    B = rng.standard_normal((nm, n, 1))
+    info, X, a1, a0, it, be = _run(A, B, V)
+    assert info == 0
+    assert it[3] == -2
+    assert it[5] in (-1, -3)
+    berr = C.backward_error(A, X, B)
+    assert (berr <= 8 * n * EPS).all()
+    # max_iter = 0: any lane whose FP32 solution is not already FP64-accurate falls back
+    info, X, a1, a0, it, be = _run(A, B, V, max_iter=0)
+    assert info == 0 and (it[it < 0] == -3).sum() + (it == -2).sum() + (it == -1).sum() == (it < 0).sum()
+    assert (C.backward_error(A, X, B) <= 8 * n * EPS).all()
+
+
+def test_refined_argument_checks(cuda):
+    import cbk_gb300
+    f = cbk_gb300.dposv_refined_compact
+    assert f("X", "L", 8, 1, None, 8, None, 8, 32, 64) == -1
+    assert f("C", "L", 8, 1, None, 8, None, 8, 32, 64, max_iter=-1) == -11
+    assert f("C", "L", 20, 1, None, 20, None, 20, 32, 64, work=0, lwork=0) == -15
+    assert f("C", "L", 0, 1, None, 1, None, 1, 32, 64) == 0
+    assert cbk_gb300.dposv_refined_lwork(8, 1, 32, 64) == 0
+    assert cbk_gb300.dposv_refined_lwork(20, 1, 32, 64) > 20 * 20 * 4 * 64
