@@ -208,17 +208,32 @@ def run_reference(args):
 # GPU
 # ---------------------------------------------------------------------------
 
+def haar_dev(cbk, n, nm, gen, device):
+    """Haar-random orthogonal U (nm, n, n) on the device: the Q of a Gaussian's
+    QR with the signs of R's diagonal folded in (Mezzadri 2007), the QR taken
+    by this library's own dgeqrf_compact + dorgqr_compact."""
+    import torch
+    G = torch.randn(nm, n, n, dtype=torch.float64, device=device, generator=gen)
+    gp = pack_dev(cbk, G)
+    del G
+    tau = torch.empty(((nm + V - 1) // V) * V * n, dtype=torch.float64, device=device)
+    cbk.check("geqrf", cbk.dgeqrf_compact("C", n, n, gp, n, tau, V, nm))
+    ng = (nm + V - 1) // V
+    d = torch.sign(gp.view(ng, n, n, V)[:, torch.arange(n), torch.arange(n), :])  # (ng, n, V)
+    d[d == 0] = 1
+    cbk.check("orgqr", cbk.dorgqr_compact("C", n, n, n, gp, n, tau, V, nm))
+    Q = gp.view(ng, n, n, V).permute(0, 3, 2, 1).reshape(ng * V, n, n)[:nm]  # [k, i, j]
+    return Q * d.permute(0, 2, 1).reshape(ng * V, n)[:nm, None, :]
+
+
 def gen_batch(n, nm, gen, device):
     """Dense A (nm, n, n) FP64 on the device and b (nm, n, 1), as the docstring
     describes."""
     import torch
+
+    import cbk_gb300 as cbk
     f64 = torch.float64
-    G = torch.randn(nm, n, n, dtype=f64, device=device, generator=gen)
-    Q, R = torch.linalg.qr(G)
-    d = torch.sign(torch.diagonal(R, dim1=1, dim2=2))
-    d[d == 0] = 1
-    U = Q * d[:, None, :]
-    del G, Q, R
+    U = haar_dev(cbk, n, nm, gen, device)
     lk = torch.empty(nm, dtype=f64, device=device).uniform_(*LOG10_KAPPA, generator=gen)
     u = torch.sort(torch.rand(nm, n, dtype=f64, device=device, generator=gen), dim=1).values
     if n > 1:

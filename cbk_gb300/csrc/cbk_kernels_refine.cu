@@ -159,55 +159,61 @@ __global__ void __launch_bounds__(128)
             for (int i = c; i < N; ++i)
                 L[tix(i, c, N)] = fmaf(-L[tix(i, j, N)], L[tix(c, j, N)], L[tix(i, c, N)]);
     }
+    // every quantity that only steers the iteration (norms, the stopping test,
+    // the reported backward error) is kept in FP32: the FP64 pipe is left to
+    // the residual itself and the FP64 update of x
     const double cte = (double)anorm * EPS64 * sqrt((double)N);
     int it_max = 0, col = 0;
-    double worst = 0.0;
+    float worst = 0.f;
     for (; col < nrhs && status == 0; ++col) {
         double x[N];
-        float z[N];
-        double bnorm = 0.0;
+        float z[N], x32[N];
+        float bnorm = 0.f;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-            const double b = B(i, col);
-            bnorm = fmax(bnorm, fabs(b));
-            z[i] = (float)b;
+            z[i] = (float)B(i, col);
+            bnorm = fmaxf(bnorm, fabsf(z[i]));
         }
         solve32<N>(L, rinv, z);
 #pragma unroll
-        for (int i = 0; i < N; ++i)
+        for (int i = 0; i < N; ++i) {
             x[i] = (double)z[i];
-        double rprev = INFINITY;
+            x32[i] = z[i];
+        }
+        float rprev = INFINITY;
         for (int it = 0;; ++it) {
             // opaque strides: the n^2 addresses of A are recomputed each step
             // (cheap integer work) instead of being hoisted into registers
             LV<double> Ar = A;
             asm volatile("" : "+l"(Ar.si), "+l"(Ar.sj));
-            double rnorm = 0.0, xnorm = 0.0;
+            float rnorm = 0.f, xnorm = 0.f;
 #pragma unroll
             for (int i = 0; i < N; ++i) {
                 double acc = B(i, col);
 #pragma unroll
                 for (int j = 0; j < N; ++j)
                     acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
-                rnorm = fmax(rnorm, fabs(acc));
-                xnorm = fmax(xnorm, fabs(x[i]));
                 z[i] = (float)acc;
+                rnorm = fmaxf(rnorm, fabsf(z[i]));
+                xnorm = fmaxf(xnorm, fabsf(x32[i]));
             }
-            if (rnorm <= cte * xnorm) {
-                const double den = (double)anorm * xnorm + bnorm;
-                worst = fmax(worst, den > 0.0 ? rnorm / den : 0.0);
+            if ((double)rnorm <= cte * (double)xnorm) {
+                const float den = anorm * xnorm + bnorm;
+                worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
                 it_max = max(it_max, it);
                 break;
             }
-            if (it >= out.max_iter || !(rnorm <= 0.5 * rprev)) {
+            if (it >= out.max_iter || !(rnorm <= 0.5f * rprev)) {
                 status = -3;
                 break;
             }
             rprev = rnorm;
             solve32<N>(L, rinv, z);
 #pragma unroll
-            for (int i = 0; i < N; ++i)
+            for (int i = 0; i < N; ++i) {
                 x[i] += (double)z[i];
+                x32[i] += z[i];
+            }
         }
         if (status == 0) {
 #pragma unroll
@@ -216,7 +222,7 @@ __global__ void __launch_bounds__(128)
         }
     }
     if (status != 0) fallback_lane(N, nrhs, status == -3 ? col - 1 : 0, A, B);
-    write_status(out, idx, status, it_max, worst);
+    write_status(out, idx, status, it_max, (double)worst);
 }
 
 // ---------------------------------------------------------------------
@@ -229,7 +235,46 @@ struct RefineWork {
     float *z;   // n per lane
 };
 
-__global__ void __launch_bounds__(128)
+// Rows i0 .. i0+NR-1 of r = b - A x in FP64, four independent accumulators
+// (A symmetric, lower triangle of the view: A(i,j) for j <= i, A(j,i) above),
+// each x_j loaded once for the NR rows. The rounded residual goes to Z; its
+// largest magnitude (FP32) is folded into rnorm.
+template <int NR>
+__device__ __forceinline__ void resid_rows(int n, int i0, int col, LV<double> A, LV<double> B,
+                                           const double *X, float *Z, int V, float &rnorm)
+{
+    double acc[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+        acc[r] = B(i0 + r, col);
+    for (int j = 0; j < i0; ++j) {
+        const double xj = X[(long)j * V];
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            acc[r] = fma(-A(i0 + r, j), xj, acc[r]);
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+        const double xj = X[(long)(i0 + c) * V];
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            acc[r] = fma(-(c <= r ? A(i0 + r, i0 + c) : A(i0 + c, i0 + r)), xj, acc[r]);
+    }
+    for (int j = i0 + NR; j < n; ++j) {
+        const double xj = X[(long)j * V];
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            acc[r] = fma(-A(j, i0 + r), xj, acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        const float z = (float)acc[r];
+        Z[(long)(i0 + r) * V] = z;
+        rnorm = fmaxf(rnorm, fabsf(z));
+    }
+}
+
+__global__ void __launch_bounds__(128, 4)
     k_posv_refined_ws(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
                       int ldbp, int V, long ngroups, size_t sa, size_t sb, RefineWork w,
                       RefineOut out)
@@ -266,53 +311,62 @@ __global__ void __launch_bounds__(128)
         for (int i = 0; i < n; ++i)
             if (!(W(i, i) > 0.f)) status = -1;
     }
+    // the norms, the stopping test and the reported backward error are FP32
+    // (they only steer the iteration); the FP64 pipe does the residual and x
     const double cte = (double)anorm * EPS64 * sqrt((double)n);
     int it_max = 0, col = 0;
-    double worst = 0.0;
+    float worst = 0.f;
     for (; col < nrhs && status == 0; ++col) {
-        double bnorm = 0.0;
+        float bnorm = 0.f;
         for (int i = 0; i < n; ++i) {
-            const double b = B(i, col);
-            bnorm = fmax(bnorm, fabs(b));
-            Z[(long)i * V] = (float)b;
+            const float b = (float)B(i, col);
+            bnorm = fmaxf(bnorm, fabsf(b));
+            Z[(long)i * V] = b;
         }
         sym_solve_block<float, false, 1>(n, W, Zv, 0);
-        for (int i = 0; i < n; ++i)
-            X[(long)i * V] = (double)Z[(long)i * V];
-        double rprev = INFINITY;
+        float xnorm = 0.f;
+        for (int i = 0; i < n; ++i) {
+            const float z = Z[(long)i * V];
+            X[(long)i * V] = (double)z;
+            xnorm = fmaxf(xnorm, fabsf(z));
+        }
+        float rprev = INFINITY;
         for (int it = 0;; ++it) {
-            double rnorm = 0.0, xnorm = 0.0;
-            for (int i = 0; i < n; ++i) {
-                double acc = B(i, col);
-                for (int j = 0; j <= i; ++j)
-                    acc = fma(-A(i, j), X[(long)j * V], acc);
-                for (int j = i + 1; j < n; ++j)
-                    acc = fma(-A(j, i), X[(long)j * V], acc);
-                rnorm = fmax(rnorm, fabs(acc));
-                xnorm = fmax(xnorm, fabs(X[(long)i * V]));
-                Z[(long)i * V] = (float)acc;
+            float rnorm = 0.f;
+            int i0 = 0;
+            for (; i0 + 4 <= n; i0 += 4)
+                resid_rows<4>(n, i0, col, A, B, X, Z, V, rnorm);
+            switch (n - i0) {
+            case 3: resid_rows<3>(n, i0, col, A, B, X, Z, V, rnorm); break;
+            case 2: resid_rows<2>(n, i0, col, A, B, X, Z, V, rnorm); break;
+            case 1: resid_rows<1>(n, i0, col, A, B, X, Z, V, rnorm); break;
+            default: break;
             }
-            if (rnorm <= cte * xnorm) {
-                const double den = (double)anorm * xnorm + bnorm;
-                worst = fmax(worst, den > 0.0 ? rnorm / den : 0.0);
+            if ((double)rnorm <= cte * (double)xnorm) {
+                const float den = anorm * xnorm + bnorm;
+                worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
                 it_max = max(it_max, it);
                 break;
             }
-            if (it >= out.max_iter || !(rnorm <= 0.5 * rprev)) {
+            if (it >= out.max_iter || !(rnorm <= 0.5f * rprev)) {
                 status = -3;
                 break;
             }
             rprev = rnorm;
             sym_solve_block<float, false, 1>(n, W, Zv, 0);
-            for (int i = 0; i < n; ++i)
-                X[(long)i * V] += (double)Z[(long)i * V];
+            xnorm = 0.f;
+            for (int i = 0; i < n; ++i) {
+                const double xi = X[(long)i * V] + (double)Z[(long)i * V];
+                X[(long)i * V] = xi;
+                xnorm = fmaxf(xnorm, fabsf((float)xi));
+            }
         }
         if (status == 0)
             for (int i = 0; i < n; ++i)
                 B(i, col) = X[(long)i * V];
     }
     if (status != 0) fallback_lane(n, nrhs, status == -3 ? col - 1 : 0, A, B);
-    write_status(out, idx, status, it_max, worst);
+    write_status(out, idx, status, it_max, (double)worst);
 }
 
 inline size_t align256(size_t b)
