@@ -425,6 +425,23 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                         work, lwork, S(st));
 }
 
+// The refined solve for callers that cannot allocate: scratch from the
+// library's fixed array; a batch whose scratch would not fit is rejected as an
+// illegal nm (-10).
+int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, int nrhs,
+                                                 double *ap, int ldap, double *bp, int ldbp, int V,
+                                                 int nm, int max_iter, int *iters, double *berr,
+                                                 cbk_stream_t st)
+{
+    bool row, up;
+    if (int e = sym_solve_args(layout, uplo, n, nrhs, ldap, ldbp, V, nm, row, up)) return e;
+    if (max_iter < 0) return -11;
+    if (n == 0 || nm == 0 || nrhs == 0) return 0;
+    if (posv_refined_lwork(n, nrhs, V, nm) > (size_t)CBK_CUDA_NOALLOC_SCRATCH_BYTES) return -10;
+    return cuda_status(launch_posv_refined_noalloc(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
+                                                   max_iter, iters, berr, S(st)));
+}
+
 CBK_CUDA_ENTRY_POINTS(double, d)
 CBK_CUDA_ENTRY_POINTS(float, s)
 

@@ -31,6 +31,9 @@
 #include "cbk_device.cuh"
 #include "cbk_launch.h"
 
+#include "../../include/cbk_cuda.h"
+
+#include <atomic>
 #include <float.h>
 #include <math.h>
 
@@ -422,6 +425,59 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
     k_posv_refined_ws<<<bl, th, 0, s>>>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, ng, sa, sb, w,
                                         out);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
+// Scratch for callers that cannot allocate device memory
+// ---------------------------------------------------------------------
+// cbk_cuda_dposv_refined_compact_noalloc_async takes no workspace: for
+// n > 16 the FP32 factor, x and the correction live in this one array,
+// reserved on every GPU that loads the library for as long as the process
+// runs. Host code cannot use the array's name as a device address, so the
+// address is looked up once per device, with that device current, and passed
+// to the kernel. Every call shares the array and nothing in it needs to start
+// at zero: the kernel writes each element it reads (the FP32 copy of A before
+// the factorization, x and the correction before each use).
+
+namespace {
+
+static_assert(CBK_CUDA_NOALLOC_SCRATCH_BYTES % 256 == 0, "scratch size");
+__device__ __align__(256) unsigned char g_noalloc_scratch[CBK_CUDA_NOALLOC_SCRATCH_BYTES];
+
+constexpr int MAX_DEVICES = 64;
+std::atomic<void *> g_noalloc_addr[MAX_DEVICES];
+
+// The device address of the scratch array on the current device (looked up on
+// the first call per device, which should come before any stream capture).
+cudaError_t noalloc_scratch(void **out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    void *p = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    if (p == nullptr) {
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev].store(p, std::memory_order_release);
+    }
+    *out = p;
+    return cudaSuccess;
+}
+
+} // namespace
+
+cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                        double *bp, int ldbp, int V, int nm, int max_iter,
+                                        int *iters, double *berr, cudaStream_t s)
+{
+    void *work = nullptr;
+    if (posv_refined_lwork(n, nrhs, V, nm) > 0) {
+        const cudaError_t e = noalloc_scratch(&work);
+        if (e != cudaSuccess) return e;
+    }
+    return launch_posv_refined(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter, iters, berr,
+                               work, s);
 }
 
 } // namespace cbkcuda

@@ -70,5 +70,9 @@ size_t posv_refined_lwork(int n, int nrhs, int V, int nm);
 cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                 double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
                                 double *berr, void *work, cudaStream_t s);
+// the same with the library's own scratch array (no allocation, no workspace)
+cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                        double *bp, int ldbp, int V, int nm, int max_iter,
+                                        int *iters, double *berr, cudaStream_t s);
 
 } // namespace cbkcuda

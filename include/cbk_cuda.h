@@ -248,6 +248,33 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                                          int max_iter, int *iters, double *berr, void *work,
                                          long long lwork, cbk_stream_t stream);
 
+/* The mixed-precision SPD solve without a workspace and without allocating.
+ * No counterpart in the reference, whose routines need no scratch memory.
+ * It is for callers that cannot allocate device memory at the point of the
+ * call: code hosted by a framework or plugin host that owns every device
+ * allocation, or a latency-bound loop that must not call cudaMalloc or
+ * cudaFree. For n > 16 the FP32 factor needs scratch; here it comes from one
+ * array of CBK_CUDA_NOALLOC_SCRATCH_BYTES (64 MiB) that the library reserves
+ * on every GPU it is used on, for as long as the process runs. n <= 16 needs
+ * none.
+ * Arguments, results and return codes are those of
+ * cbk_cuda_dposv_refined_compact_async without work and lwork, plus -10 when
+ * the batch is too large for the array: when
+ * cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) exceeds
+ * CBK_CUDA_NOALLOC_SCRATCH_BYTES (for n = 48, about 6,800 matrices; split
+ * larger batches into several calls).
+ * The first call on a device looks up the array's device address with that
+ * device current: make that first call before any stream capture. Every call
+ * shares the one array, and it keeps the last call's contents; nothing in it
+ * needs to start at zero. Calls that overlap on the GPU -- on different
+ * streams, or from host threads without ordering between them -- race on the
+ * array and give wrong results: serialise them on one stream. */
+#define CBK_CUDA_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, int nrhs,
+                                                 double *ap, int ldap, double *bp, int ldbp,
+                                                 int V, int nm, int max_iter, int *iters,
+                                                 double *berr, cbk_stream_t stream);
+
 /* Calibration, no reference counterpart: the measured fused multiply-add
  * rate of the current device in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1)
  * or FP32 (fp64 = 0), from a ~10 ms synthetic kernel -- the denominator of the
