@@ -520,6 +520,178 @@ def e2e(args, cbk, batches, barrier, ws):
                     "D2H, per n"}
 
 
+# ---------------------------------------------------------------------------
+# the other configurations (--config): one JSON line each, same timing rules
+# ---------------------------------------------------------------------------
+
+def _timer(dev):
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def run(fn, restore, K, W):
+        ts = []
+        for k in range(W + K):
+            restore()
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            n_launch = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if k >= W:
+                ts.append(e0.elapsed_time(e1))
+        return sum(ts) / len(ts), n_launch
+    return run
+
+
+def run_config(args):
+    import numpy as np
+    import torch
+
+    import cbk_gb300 as cbk
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    timed = _timer(dev)
+    f64 = torch.float64
+    line = {"metric": None, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": None, "l2": "flushed (256 MiB write) before every timed step",
+                       "inputs": "restored untimed before every step"}}
+    if args.config == "c1":
+        n, nm = 8, 65536
+        G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
+        A = G @ G.transpose(1, 2) + n * torch.eye(n, dtype=f64, device=dev)
+        B = torch.randn(nm, n, 1, dtype=f64, device=dev, generator=gen)
+        ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+        ap, bp = ap0.clone(), bp0.clone()
+
+        def restore():
+            ap.copy_(ap0)
+            bp.copy_(bp0)
+        t, _ = timed(lambda: cbk.check("posv", cbk.dposv_compact("C", "L", n, 1, ap, n, bp, n, V,
+                                                                 nm)) or 1, restore,
+                     args.steps, args.warmup)
+        berr = berr_max(A, x_dense(bp, n, nm), B) / (n * 2.220446049250313e-16)
+        it = torch.empty(nm, dtype=torch.int32, device=dev)
+        tr, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
+            "C", "L", n, 1, ap, n, bp, n, V, nm, 10, it)) or 1, restore, args.steps, args.warmup)
+        line.update(metric="dposv_compact FP64 n=8 nrhs=1 solves/s", value=nm / (t * 1e-3),
+                    unit=UNIT, ms_per_step=t, dtype="f64",
+                    data="synthetic: A = G G^T + n I, G, B ~ N(0,1), seed 0x5EED",
+                    max_berr_over_n_eps=berr, refined_value=nm / (tr * 1e-3),
+                    gbs=nm * bytes_per_matrix(n) * 704 / 416 / (t * 1e-3) / 1e9,
+                    gpu_launches=args.steps)
+        line["config"]["workload"] = "dposv_compact n=8 nrhs=1, 65536 matrices, V=32"
+    elif args.config == "c2":
+        m, n, nrhs, nm = 16, 8, 4, 1 << 20
+        A = torch.randn(nm, m, n, dtype=f64, device=dev, generator=gen)
+        B = torch.randn(nm, m, nrhs, dtype=f64, device=dev, generator=gen)
+        ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+        ap, bp = ap0.clone(), bp0.clone()
+        tau = torch.empty(nm * n, dtype=f64, device=dev)
+
+        def restore():
+            ap.copy_(ap0)
+            bp.copy_(bp0)
+        t, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact("C", "N", m, n, nrhs, ap, m, bp,
+                                                                 m, tau, V, nm)) or 1,
+                     restore, args.steps, args.warmup)
+        geq = ap.clone()  # the QR left by the last gels, for orgqr
+
+        def restore_q():
+            ap.copy_(geq)
+        tq, _ = timed(lambda: cbk.check("orgqr", cbk.dorgqr_compact("C", m, n, n, ap, m, tau, V,
+                                                                    nm)) or 1,
+                      restore_q, args.steps, args.warmup)
+        ng = nm // V
+        Q = ap.view(ng, n, m, V).permute(0, 3, 2, 1).reshape(nm, m, n)
+        orth = float((Q.transpose(1, 2) @ Q - torch.eye(n, dtype=f64, device=dev)).abs()
+                     .amax()) / 2.220446049250313e-16
+        line.update(metric="dgels_compact FP64 16x8 nrhs=4 solves/s", value=nm / (t * 1e-3),
+                    unit=UNIT, ms_per_step=t, dtype="f64", data="synthetic: A, B ~ N(0,1)",
+                    gbs=nm * 3136 / (t * 1e-3) / 1e9, dorgqr_ms=tq,
+                    dorgqr_per_s=nm / (tq * 1e-3), dorgqr_orthogonality_over_eps=orth,
+                    gpu_launches=args.steps)
+        line["config"]["workload"] = "dgels_compact m=16 n=8 nrhs=4 + dorgqr, 1048576, V=32"
+    elif args.config == "c4":
+        nrhs, total = 2, 1 << 20
+        rng = np.random.default_rng(SEED)
+        counts = np.bincount(rng.integers(4, 49, total), minlength=49)[4:]
+        bks = []
+        for k, n in enumerate(range(4, 49)):
+            nm = int(counts[k])
+            G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
+            S = (G + G.transpose(1, 2)) / 2 + 2 * n * torch.eye(n, dtype=f64, device=dev)
+            Bm = torch.randn(nm, n, nrhs, dtype=f64, device=dev, generator=gen)
+            a0, b0 = pack_dev(cbk, S), pack_dev(cbk, Bm)
+            bks.append(dict(n=n, nm=nm, a0=a0, b0=b0, a=a0.clone(), b=b0.clone()))
+            del G, S, Bm
+
+        def restore():
+            for b in bks:
+                b["a"].copy_(b["a0"])
+                b["b"].copy_(b["b0"])
+        work = torch.empty(cbk.BUCKETED_LWORK, dtype=torch.uint8, device=dev)
+        tup = [(b["n"], b["nm"], V, b["a"], b["n"], b["b"], b["n"]) for b in bks]
+        graph = cbk.BucketedGraph("C", "L", nrhs, tup, work)
+        tg, _ = timed(lambda: cbk.check("graph", graph.launch()) or 1, restore, args.steps,
+                      args.warmup)
+
+        def per_size():
+            for b in bks:
+                cbk.check("sysvnp", cbk.dsysvnp_compact("C", "L", b["n"], nrhs, b["a"], b["n"],
+                                                        b["b"], b["n"], V, b["nm"]))
+            return len(bks)
+        tp, _ = timed(per_size, restore, args.steps, args.warmup)
+        graph.close()
+        line.update(metric="uneven-size dsysvnp solves/s (n~U{4..48}, nrhs=2)",
+                    value=total / (tg * 1e-3), unit=UNIT, ms_per_step=tg, dtype="f64",
+                    data="synthetic: symmetric N(0,1) + 2n I, B ~ N(0,1)",
+                    per_size_launches={"value": total / (tp * 1e-3), "ms_per_step": tp,
+                                       "launches": len(bks)},
+                    speedup_graph_vs_per_size=tp / tg, gpu_launches=args.steps)
+        line["config"]["workload"] = ("dsysvnp_compact, 1048576 matrices, n uniform in 4..48, "
+                                      "45 buckets, V=32: one persistent CUDA-graph launch")
+    elif args.config == "c5":
+        m, n, nrhs, nm = 64, 16, 8, 131072
+        rng = np.random.default_rng(SEED)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import cases as C
+        A, Bm, _, kappa = C.gen_ls_cond(rng, nm, m, n, nrhs)
+        from oracle import oracle as O
+        ap0 = torch.from_numpy(O.pack(A, V)).to(dev)
+        bp0 = torch.from_numpy(O.pack(Bm, V, pad_diag=0.0)).to(dev)
+        ap, bp = ap0.clone(), bp0.clone()
+        tau = torch.empty(nm * n, dtype=f64, device=dev)
+        it = torch.empty(nm, dtype=torch.int32, device=dev)
+        work = torch.empty(cbk.dgels_refined_lwork(m, n, nrhs, V, nm), dtype=torch.uint8,
+                           device=dev)
+
+        def restore():
+            ap.copy_(ap0)
+            bp.copy_(bp0)
+        tr, _ = timed(lambda: cbk.check("gels_refined", cbk.dgels_refined_compact(
+            "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm, 10, it, None, work)) or 1, restore,
+            args.steps, args.warmup)
+        itc = it.cpu().numpy()
+        tpl, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact("C", "N", m, n, nrhs, ap, m,
+                                                                   bp, m, tau, V, nm)) or 1,
+                       restore, args.steps, args.warmup)
+        line.update(metric="least squares 64x16 nrhs=8 solves/s: refined FP32 vs plain FP64",
+                    value=nm / (tr * 1e-3), unit=UNIT, ms_per_step=tr,
+                    dtype="f32 QR + f64 refinement", data="synthetic: A = U diag(s) V^T, kappa "
+                    "1e1..1e4, B = A X + 1e-3 N(0,1)",
+                    plain_fp64={"value": nm / (tpl * 1e-3), "ms_per_step": tpl},
+                    speedup_refined_vs_plain=tpl / tr,
+                    refinement={"converged_frac": float((itc >= 0).mean()),
+                                "mean_steps": float(itc[itc >= 0].mean())},
+                    gpu_launches=args.steps)
+        line["config"]["workload"] = "dgels m=64 n=16 nrhs=8, 131072 matrices, V=32"
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -528,11 +700,15 @@ def main():
     ap.add_argument("--impl", choices=("cbk", "reference"), default="cbk")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5"), default="c3",
+                    help="c3 (default) is the headline; the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3  # at least three untimed warm-up steps
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != "c3":
+        run_config(args)
     else:
         run_gpu(args)
 

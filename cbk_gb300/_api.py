@@ -74,3 +74,148 @@ def dposv_refined_compact(layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_
 
 
 __all__ += ["dposv_refined_compact", "dposv_refined_lwork"]
+
+
+# ---------------------------------------------------------------------------
+# uneven orders: bucketed launches and their CUDA graphs
+# ---------------------------------------------------------------------------
+
+def _bucket_struct(scalar):
+    import ctypes
+
+    class Bucket(ctypes.Structure):
+        _fields_ = [("n", ctypes.c_int), ("nm", ctypes.c_int), ("V", ctypes.c_int),
+                    ("ap", ctypes.c_void_p), ("ldap", ctypes.c_int), ("bp", ctypes.c_void_p),
+                    ("ldbp", ctypes.c_int)]
+    return Bucket
+
+
+_BUCKET = {}
+
+
+def _buckets(prefix, buckets):
+    """A ctypes array of bucket descriptors from (n, nm, V, ap, ldap, bp, ldbp)
+    tuples whose ap / bp are CUDA tensors or device pointers."""
+    from ._abi import _ptr
+    if prefix not in _BUCKET:
+        _BUCKET[prefix] = _bucket_struct(prefix)
+    B = _BUCKET[prefix]
+    arr = (B * max(1, len(buckets)))()
+    for k, (n, nm, V, ap, ldap, bp, ldbp) in enumerate(buckets):
+        arr[k] = B(n, nm, V, _ptr(ap, prefix), ldap, _ptr(bp, prefix), ldbp)
+    return arr
+
+
+BUCKETED_LWORK = 256
+
+
+def bucketed_compact(routine, prefix, layout, uplo, nrhs, buckets, work=None, stream=None):
+    """One persistent launch over buckets of single-order compact batches:
+    routine 'sysvnp' or 'posv', prefix 'd' or 's'. buckets: a list of
+    (n, nm, V, ap, ldap, bp, ldbp). work: >= 256 bytes of device memory
+    (allocated here when None). Returns the info code."""
+    import ctypes
+
+    from ._abi import _stream, lib
+    if work is None:
+        import torch
+        work = torch.empty(BUCKETED_LWORK, dtype=torch.uint8, device="cuda")
+    f = getattr(lib(), f"cbk_cuda_{prefix}{routine}_compact_bucketed_async")
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
+    arr = _buckets(prefix, buckets)
+    wptr = work if isinstance(work, int) else work.data_ptr()
+    wlen = BUCKETED_LWORK if isinstance(work, int) else work.numel() * work.element_size()
+    return f(layout.encode(), uplo.encode(), nrhs, len(buckets), ctypes.addressof(arr), wptr,
+             wlen, _stream(stream))
+
+
+class BucketedGraph:
+    """cbk_cuda_dsysvnp_compact_bucketed_graph: the bucketed launch captured
+    once into a CUDA graph; launch() replays it on a stream."""
+
+    def __init__(self, layout, uplo, nrhs, buckets, work):
+        import ctypes
+
+        from ._abi import check, lib
+        self._lib = lib()
+        f = self._lib.cbk_cuda_dsysvnp_compact_bucketed_graph
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_longlong, ctypes.POINTER(ctypes.c_void_p)]
+        arr = _buckets("d", buckets)
+        self._work = work
+        self.handle = ctypes.c_void_p()
+        check("dsysvnp_compact_bucketed_graph",
+              f(layout.encode(), uplo.encode(), nrhs, len(buckets), ctypes.addressof(arr),
+                work.data_ptr(), work.numel() * work.element_size(), ctypes.byref(self.handle)))
+
+    def launch(self, stream=None):
+        import ctypes
+
+        from ._abi import _stream
+        f = self._lib.cbk_cuda_graph_launch
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        return f(self.handle, _stream(stream))
+
+    def close(self):
+        if self.handle:
+            import ctypes
+            f = self._lib.cbk_cuda_graph_destroy
+            f.argtypes = [ctypes.c_void_p]
+            f(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+__all__ += ["bucketed_compact", "BucketedGraph", "BUCKETED_LWORK"]
+
+
+def dgels_refined_lwork(m: int, n: int, nrhs: int, V: int, nm: int) -> int:
+    """Workspace bytes of dgels_refined_compact."""
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_dgels_refined_compact_lwork
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_int] * 5
+    return int(f(m, n, nrhs, V, nm))
+
+
+def dgels_refined_compact(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
+                          max_iter=10, iters=None, berr=None, work=None, stream=None):
+    """Mixed-precision dgels for m >= n, trans 'N' (FP32 QR + FP64 refinement of
+    the augmented system, FP64 fallback per matrix). work is allocated here
+    when None (the C entry point itself never allocates)."""
+    import ctypes
+
+    from ._abi import _ptr, _stream, lib
+    need = dgels_refined_lwork(m, n, nrhs, V, nm) if min(m, n, nm, V) > 0 else 0
+    if work is None and need > 0:
+        import torch
+        work = torch.empty(need, dtype=torch.uint8, device="cuda")
+    f = lib().cbk_cuda_dgels_refined_compact_async
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_char] + [ctypes.c_int] * 3 + [
+        ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
+
+    def raw(t):
+        return t if (t is None or isinstance(t, int)) else t.data_ptr()
+    wbytes = 0 if work is None else (need if isinstance(work, int)
+                                     else work.numel() * work.element_size())
+    live = ap is not None and not isinstance(ap, int)
+    return f(layout.encode(), trans.encode(), m, n, nrhs, _ptr(ap, "d"), ldap, _ptr(bp, "d"),
+             ldbp, _ptr(taup, "d"), V, nm, max_iter, raw(iters), raw(berr), raw(work), wbytes,
+             _stream(stream) if live or stream else None)
+
+
+__all__ += ["dgels_refined_compact", "dgels_refined_lwork"]

@@ -240,6 +240,66 @@ int posv_refined(char layout, char uplo, int n, int nrhs, double *ap, int ldap, 
                                            iters, berr, work, s));
 }
 
+int gels_refined(char layout, char trans, int m, int n, int nrhs, double *ap, int ldap, double *bp,
+                 int ldbp, double *taup, int V, int nm, int max_iter, int *iters, double *berr,
+                 void *work, long long lwork, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const int mx = m > n ? m : n;
+    if (!col && !row) return -1;
+    if (!opt(trans, 'N')) return -2; // the refined path solves A X = B
+    if (m < 0) return -3;
+    if (n < 0 || n > m || n > gels_refined_nmax()) return -4;
+    if (nrhs < 0) return -5;
+    if (ldap < max1(row ? n : m)) return -7;
+    if (ldbp < max1(row ? nrhs : mx)) return -9;
+    if (!vlen_ok(V)) return -11;
+    if (nm < 0) return -12;
+    if (max_iter < 0) return -13;
+    if (nrhs == 0 || nm == 0 || m == 0) return 0;
+    if (n == 0) return cuda_status(launch_zero<double>(row, m, nrhs, bp, ldbp, V, nm, s));
+    const size_t need = gels_refined_lwork(m, n, nrhs, V, nm);
+    if (work == nullptr || lwork < (long long)need) return -17;
+    return cuda_status(launch_gels_refined(row, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
+                                           max_iter, iters, berr, work, s));
+}
+
+template <typename T, typename Bucket>
+int bucketed(bool ldlt, char layout, char uplo, int nrhs, int nbuckets, const Bucket *bk,
+             void *work, long long lwork, cudaStream_t s)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    const bool lo = opt(uplo, 'L'), up = opt(uplo, 'U');
+    if (!col && !row) return -1;
+    if (!lo && !up) return -2;
+    if (nrhs < 0) return -3;
+    if (nbuckets < 0 || nbuckets > CBK_CUDA_MAX_BUCKETS) return -4;
+    if (nbuckets > 0 && bk == nullptr) return -5;
+    int n[CBK_CUDA_MAX_BUCKETS], nm[CBK_CUDA_MAX_BUCKETS], V[CBK_CUDA_MAX_BUCKETS];
+    int lda[CBK_CUDA_MAX_BUCKETS], ldb[CBK_CUDA_MAX_BUCKETS];
+    T *ap[CBK_CUDA_MAX_BUCKETS], *bp[CBK_CUDA_MAX_BUCKETS];
+    bool any = false;
+    for (int b = 0; b < nbuckets; ++b) {
+        const Bucket &e = bk[b];
+        if (e.n < 0 || e.nm < 0 || !vlen_ok(e.V) || e.ldap < max1(e.n) ||
+            e.ldbp < max1(row ? nrhs : e.n))
+            return -5;
+        n[b] = e.n;
+        nm[b] = e.nm;
+        V[b] = e.V;
+        lda[b] = e.ldap;
+        ldb[b] = e.ldbp;
+        ap[b] = e.ap;
+        bp[b] = e.bp;
+        any = any || (e.n > 0 && e.nm > 0);
+    }
+    if (work == nullptr) return -6;
+    if (lwork < CBK_CUDA_BUCKETED_LWORK) return -7;
+    if (!any) return 0;
+    return cuda_status(
+        launch_bucketed<T>(ldlt, row, up, nrhs, nbuckets, n, nm, V, ap, lda, bp, ldb, work, s));
+}
+
 inline cudaStream_t S(cbk_stream_t s)
 {
     return reinterpret_cast<cudaStream_t>(s);
@@ -440,6 +500,100 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
     if (posv_refined_lwork(n, nrhs, V, nm) > (size_t)CBK_CUDA_NOALLOC_SCRATCH_BYTES) return -10;
     return cuda_status(launch_posv_refined_noalloc(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
                                                    max_iter, iters, berr, S(st)));
+}
+
+long long cbk_cuda_dgels_refined_compact_lwork(int m, int n, int nrhs, int V, int nm)
+{
+    if (m < 0 || n < 0 || nrhs < 0 || !vlen_ok(V) || nm < 0) return -1;
+    return (long long)gels_refined_lwork(m, n, nrhs, V, nm);
+}
+
+int cbk_cuda_dgels_refined_compact_async(char layout, char trans, int m, int n, int nrhs,
+                                         double *ap, int ldap, double *bp, int ldbp,
+                                         double *taup, int V, int nm, int max_iter, int *iters,
+                                         double *berr, void *work, long long lwork,
+                                         cbk_stream_t st)
+{
+    return gels_refined(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, max_iter,
+                        iters, berr, work, lwork, S(st));
+}
+
+int cbk_cuda_dsysvnp_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_dbucket *buckets, void *work,
+                                            long long lwork, cbk_stream_t st)
+{
+    return bucketed<double>(true, layout, uplo, nrhs, nbuckets, buckets, work, lwork, S(st));
+}
+int cbk_cuda_ssysvnp_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_sbucket *buckets, void *work,
+                                            long long lwork, cbk_stream_t st)
+{
+    return bucketed<float>(true, layout, uplo, nrhs, nbuckets, buckets, work, lwork, S(st));
+}
+int cbk_cuda_dposv_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                          const cbk_cuda_dbucket *buckets, void *work,
+                                          long long lwork, cbk_stream_t st)
+{
+    return bucketed<double>(false, layout, uplo, nrhs, nbuckets, buckets, work, lwork, S(st));
+}
+int cbk_cuda_sposv_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                          const cbk_cuda_sbucket *buckets, void *work,
+                                          long long lwork, cbk_stream_t st)
+{
+    return bucketed<float>(false, layout, uplo, nrhs, nbuckets, buckets, work, lwork, S(st));
+}
+
+struct cbk_cuda_graph_st {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+int cbk_cuda_dsysvnp_compact_bucketed_graph(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_dbucket *buckets, void *work,
+                                            long long lwork, cbk_cuda_graph *graph)
+{
+    if (graph == nullptr) return -8;
+    *graph = nullptr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return cuda_status(e);
+    }
+    const int info = bucketed<double>(true, layout, uplo, nrhs, nbuckets, buckets, work, lwork, s);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(s, &g);
+    cudaStreamDestroy(s);
+    if (info != 0) {
+        if (g) cudaGraphDestroy(g);
+        return info;
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    cudaGraphExec_t x = nullptr;
+    e = cudaGraphInstantiate(&x, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_status(e);
+    }
+    *graph = new cbk_cuda_graph_st{g, x};
+    return 0;
+}
+
+int cbk_cuda_graph_launch(cbk_cuda_graph graph, cbk_stream_t st)
+{
+    if (graph == nullptr) return -1;
+    return cuda_status(cudaGraphLaunch(graph->exec, S(st)));
+}
+
+int cbk_cuda_graph_destroy(cbk_cuda_graph graph)
+{
+    if (graph == nullptr) return 0;
+    cudaError_t e1 = cudaGraphExecDestroy(graph->exec);
+    cudaError_t e2 = cudaGraphDestroy(graph->graph);
+    delete graph;
+    return cuda_status(e1 != cudaSuccess ? e1 : e2);
 }
 
 CBK_CUDA_ENTRY_POINTS(double, d)

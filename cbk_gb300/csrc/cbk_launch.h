@@ -70,6 +70,20 @@ size_t posv_refined_lwork(int n, int nrhs, int V, int nm);
 cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                 double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
                                 double *berr, void *work, cudaStream_t s);
+// mixed-precision least squares (cbk_kernels_refine_gels.cu)
+size_t gels_refined_lwork(int m, int n, int nrhs, int V, int nm);
+int gels_refined_nmax();
+cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, int ldap, double *bp,
+                                int ldbp, double *taup, int V, int nm, int max_iter, int *iters,
+                                double *berr, void *work, cudaStream_t s);
+
+// one persistent launch over a table of single-order compact buckets
+// (cbk_kernels_bucketed.cu); work holds the 8-byte item counter
+template <typename T>
+cudaError_t launch_bucketed(bool ldlt, bool row, bool up, int nrhs, int nbuckets, const int *n,
+                            const int *nm, const int *V, T *const *ap, const int *ldap,
+                            T *const *bp, const int *ldbp, void *work, cudaStream_t s);
+
 // the same with the library's own scratch array (no allocation, no workspace)
 cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                         double *bp, int ldbp, int V, int nm, int max_iter,

@@ -248,6 +248,93 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                                          int max_iter, int *iters, double *berr, void *work,
                                          long long lwork, cbk_stream_t stream);
 
+/* Mixed-precision least squares min ||b - A x||, A m x n with m >= n: FP32
+ * QR, FP64 refinement of the augmented system [I A; A^T 0][r; x] = [b; 0]
+ * (Bjorck) per right-hand side, FP64 fallback per matrix. No reference entry
+ * point: the ?gels_compact arguments (include/cbk.h:335-351) for the
+ * overdetermined, non-transposed case. Per lane: x0 from the FP32 QR, then
+ * f = b - r - A x and g = -A^T r in FP64, the correction from the FP32 QR,
+ * until both residuals are at the FP64 rounding level of their terms
+ * (||g||_inf <= sqrt(n) eps64 ||A|| (||A|| ||x|| + ||b|| + ||r||) and
+ * ||f||_inf <= sqrt(n) eps64 (||A|| ||x|| + ||b|| + ||r||)). A lane whose FP32 rounding
+ * overflows (iters -2) or whose refinement stalls or exceeds max_iter (-3)
+ * is solved by the FP64 path, whose QR then sits in ap and taup; a converged
+ * lane leaves ap and taup untouched. On exit B(0:n) holds X and B(n:m) the
+ * residual's coordinates (Q^T r)(n:m) through the FP32 Q (their squared
+ * norms are the residual sums of squares to FP32 accuracy).
+ *   iters, berr  device int[nm] / double[nm] or NULL: corrections used, or
+ *          the fallback code; the largest normal-equations residual
+ *          ||A^T r||_inf / (||A||_inf (||A||_inf ||x||_inf + ||b||_inf))
+ *          (NaN when the lane fell back)
+ *   work   at least cbk_cuda_dgels_refined_compact_lwork(m, n, nrhs, V, nm)
+ *          bytes of device memory
+ * Returns 0, or -j: -1 layout -2 trans (only 'N') -3 m -4 n (< 0, > m or
+ * > 64) -5 nrhs -7 ldap -9 ldbp -11 V -12 nm -13 max_iter -17 lwork.
+ * nrhs = 0, nm = 0 or m = 0 return at once; n = 0 sets B := 0. */
+long long cbk_cuda_dgels_refined_compact_lwork(int m, int n, int nrhs, int V, int nm);
+int cbk_cuda_dgels_refined_compact_async(char layout, char trans, int m, int n, int nrhs,
+                                         double *ap, int ldap, double *bp, int ldbp,
+                                         double *taup, int V, int nm, int max_iter, int *iters,
+                                         double *berr, void *work, long long lwork,
+                                         cbk_stream_t stream);
+
+/* Batches of uneven orders in one persistent launch. No reference counterpart:
+ * the reference takes one order per call (?sysvnp_compact, ?posv_compact), so
+ * a mixed batch is one call per order. Here the caller groups the matrices by
+ * order into buckets, each an ordinary compact batch (its own n, nm, V, ap,
+ * ldap, bp, ldbp, the layout of include/cbk.h), and one launch factors and
+ * solves every bucket: the work is cut into 32-lane items, largest order
+ * first, pulled by one wave of warps from a device counter held in `work`.
+ * Each bucket's results are bit-identical to a ?sysvnp_compact
+ * (?posv_compact) call on that bucket alone; nrhs = 0 factors only.
+ *   work   device memory of at least CBK_CUDA_BUCKETED_LWORK bytes (the item
+ *          counter; reset by the call itself -- concurrent calls need their
+ *          own work)
+ * Returns 0, or -j: -1 layout -2 uplo -3 nrhs (< 0) -4 nbuckets (< 0 or
+ * > CBK_CUDA_MAX_BUCKETS) -5 buckets (NULL, or an entry with n < 0, nm < 0,
+ * an illegal V, ldap < max(1, n), or ldbp < max(1, n) column-major /
+ * max(1, nrhs) row-major) -6 work (NULL) -7 lwork (too small). */
+#define CBK_CUDA_MAX_BUCKETS 64
+#define CBK_CUDA_BUCKETED_LWORK 256
+typedef struct {
+    int n, nm, V;
+    double *ap;
+    int ldap;
+    double *bp;
+    int ldbp;
+} cbk_cuda_dbucket;
+typedef struct {
+    int n, nm, V;
+    float *ap;
+    int ldap;
+    float *bp;
+    int ldbp;
+} cbk_cuda_sbucket;
+int cbk_cuda_dsysvnp_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_dbucket *buckets, void *work,
+                                            long long lwork, cbk_stream_t stream);
+int cbk_cuda_ssysvnp_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_sbucket *buckets, void *work,
+                                            long long lwork, cbk_stream_t stream);
+int cbk_cuda_dposv_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                          const cbk_cuda_dbucket *buckets, void *work,
+                                          long long lwork, cbk_stream_t stream);
+int cbk_cuda_sposv_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,
+                                          const cbk_cuda_sbucket *buckets, void *work,
+                                          long long lwork, cbk_stream_t stream);
+
+/* The same launch captured once into an instantiated CUDA graph (the counter
+ * reset and the persistent kernel), replayed by cbk_cuda_graph_launch on any
+ * stream: one submission per replay, no host work. The buckets' pointers are
+ * baked in; the graph is valid while they are. graph_create returns the
+ * bucketed call's codes (-1 .. -7), or CBK_CUDA_ERROR_BASE + a CUDA error. */
+typedef struct cbk_cuda_graph_st *cbk_cuda_graph;
+int cbk_cuda_dsysvnp_compact_bucketed_graph(char layout, char uplo, int nrhs, int nbuckets,
+                                            const cbk_cuda_dbucket *buckets, void *work,
+                                            long long lwork, cbk_cuda_graph *graph);
+int cbk_cuda_graph_launch(cbk_cuda_graph graph, cbk_stream_t stream);
+int cbk_cuda_graph_destroy(cbk_cuda_graph graph);
+
 /* The mixed-precision SPD solve without a workspace and without allocating.
  * No counterpart in the reference, whose routines need no scratch memory.
  * It is for callers that cannot allocate device memory at the point of the

@@ -422,3 +422,20 @@ def backward_error(A, X, B):
     bn = np.abs(B).max(axis=1)
     den = an[:, None] * xn + bn
     return np.where(den > 0, rn / np.where(den > 0, den, 1), 0).max(axis=1)
+
+
+def gen_ls_cond(rng, nm, m, n, nrhs, log10_kappa=(1.0, 4.0), noise=1e-3):
+    """A = U diag(s) V^T (U Haar m x n thin, V Haar n x n), s log-uniform with
+    log10 kappa uniform in log10_kappa; B = A X + noise * N(0,1), X ~ N(0,1).
+    Returns (A, B, X, kappa)."""
+    kappa = 10.0 ** rng.uniform(*log10_kappa, nm)
+    u = np.sort(rng.uniform(0, 1, (nm, n)), axis=1)
+    if n > 1:
+        u[:, 0], u[:, -1] = 0.0, 1.0
+    s = kappa[:, None] ** (-u)
+    U = haar(rng, nm, m, n)
+    Vh = haar(rng, nm, n)
+    A = (U * s[:, None, :]) @ Vh.transpose(0, 2, 1)
+    X = rng.standard_normal((nm, n, nrhs))
+    B = A @ X + noise * rng.standard_normal((nm, m, nrhs))
+    return A, B, X, kappa

@@ -96,3 +96,32 @@ def test_status_strings():
     assert cbk_gb300.status_string(0) == "success"
     assert "illegal" in cbk_gb300.status_string(-3)
     assert cbk_gb300.status_string(1002)  # a CUDA error text
+
+
+def test_bucketed_argument_checks():
+    """The bucketed entry points check their table before any device work."""
+    import ctypes
+
+    import cbk_gb300
+    from cbk_gb300._api import _buckets
+    f = cbk_gb300.lib().cbk_cuda_dsysvnp_compact_bucketed_async
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
+    ok = _buckets("d", [(8, 40, 32, 0, 8, 0, 8), (5, 3, 32, 0, 5, 0, 5)])
+    bad_ld = _buckets("d", [(8, 40, 32, 0, 8, 0, 8), (5, 3, 32, 0, 4, 0, 5)])
+    bad_v = _buckets("d", [(8, 40, 24, 0, 8, 0, 8)])
+    empty = _buckets("d", [(0, 40, 32, 0, 1, 0, 1), (6, 0, 32, 0, 6, 0, 6)])
+    a = ctypes.addressof
+    fake_work = 1 << 40  # never dereferenced: every row returns before device work
+    assert f(b"X", b"L", 2, 2, a(ok), fake_work, 256, None) == -1
+    assert f(b"C", b"X", 2, 2, a(ok), fake_work, 256, None) == -2
+    assert f(b"C", b"L", -1, 2, a(ok), fake_work, 256, None) == -3
+    assert f(b"C", b"L", 2, 65, a(ok), fake_work, 256, None) == -4
+    assert f(b"C", b"L", 2, 2, None, fake_work, 256, None) == -5
+    assert f(b"C", b"L", 2, 2, a(bad_ld), fake_work, 256, None) == -5
+    assert f(b"C", b"L", 2, 1, a(bad_v), fake_work, 256, None) == -5
+    assert f(b"C", b"L", 2, 2, a(ok), None, 256, None) == -6
+    assert f(b"C", b"L", 2, 2, a(ok), fake_work, 255, None) == -7
+    assert f(b"C", b"L", 2, 2, a(empty), fake_work, 256, None) == 0
+    assert f(b"C", b"L", 2, 0, None, fake_work, 256, None) == 0
