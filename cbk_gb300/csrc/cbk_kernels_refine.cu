@@ -24,8 +24,10 @@
 // per right-hand side falls from n^3/6 + n^2 fused multiply-adds and 2n long
 // operations to n^2 per refinement step.
 //
-// Two variants: orders up to 16 keep the FP32 factor and x in registers
-// (compile-time order); larger orders keep the FP32 factor, x and the
+// Three variants: orders up to 16 keep the FP32 factor and x in registers
+// (compile-time order, one thread per matrix, below); orders 17 .. 64 run one
+// warp per matrix with the matrix staged in shared memory
+// (cbk_kernels_refine_warp.cu); larger orders keep the FP32 factor, x and the
 // correction in the caller's workspace, in the compact layout (coalesced),
 // sized by cbk_cuda_dposv_refined_compact_lwork.
 #include "cbk_device.cuh"
@@ -383,7 +385,7 @@ inline size_t align256(size_t b)
 size_t posv_refined_lwork(int n, int nrhs, int V, int nm)
 {
     (void)nrhs;
-    if (n <= REG_NMAX || nm <= 0) return 0;
+    if (n <= REG_NMAX || posv_refined_warp_ok(n) || nm <= 0) return 0;
     const size_t lanes = (size_t)((nm + V - 1) / V) * V;
     return align256(lanes * (size_t)n * n * sizeof(float)) +
            align256(lanes * (size_t)n * sizeof(double)) + align256(lanes * (size_t)n * sizeof(float));
@@ -414,6 +416,9 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
         }
         return cudaGetLastError();
     }
+    if (posv_refined_warp_ok(n))
+        return launch_posv_refined_warp(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter,
+                                        iters, berr, s);
     const size_t lanes = (size_t)ng * V;
     char *base = static_cast<char *>(work);
     RefineWork w;
@@ -431,7 +436,7 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
 // Scratch for callers that cannot allocate device memory
 // ---------------------------------------------------------------------
 // cbk_cuda_dposv_refined_compact_noalloc_async takes no workspace: for
-// n > 16 the FP32 factor, x and the correction live in this one array,
+// n > 64 the FP32 factor, x and the correction live in this one array,
 // reserved on every GPU that loads the library for as long as the process
 // runs. Host code cannot use the array's name as a device address, so the
 // address is looked up once per device, with that device current, and passed

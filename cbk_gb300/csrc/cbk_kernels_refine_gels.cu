@@ -50,7 +50,7 @@ struct GelsWork {
     double *r;  // m per lane: the FP64 residual estimate
 };
 
-__device__ __noinline__ void gels_fallback(int m, int n, int nrhs, int first, LV<double> A,
+__device__ __forceinline__ void gels_fallback(int m, int n, int nrhs, int first, LV<double> A,
                                            double *taup, int V, LV<double> B)
 {
     geqrf_lane<double>(m, n, A, taup, V);

@@ -84,6 +84,12 @@ cudaError_t launch_bucketed(bool ldlt, bool row, bool up, int nrhs, int nbuckets
                             const int *nm, const int *V, T *const *ap, const int *ldap,
                             T *const *bp, const int *ldbp, void *work, cudaStream_t s);
 
+// orders 17 .. 64: one warp per matrix, no workspace (cbk_kernels_refine_warp.cu)
+bool posv_refined_warp_ok(int n);
+cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                     double *bp, int ldbp, int V, int nm, int max_iter,
+                                     int *iters, double *berr, cudaStream_t s);
+
 // the same with the library's own scratch array (no allocation, no workspace)
 cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                         double *bp, int ldbp, int V, int nm, int max_iter,

@@ -237,8 +237,10 @@ int cbk_cuda_sunpack_compact_async(char layout, int m, int n, const float *ap, i
  *          error ||b - A x|| / (||A|| ||x|| + ||b||) (inf-norms), NaN when the
  *          lane fell back
  *   work   device workspace of lwork bytes, at least
- *          cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) (0 for n <= 16,
- *          where the FP32 factor lives in registers; NULL allowed then)
+ *          cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm): 0 for n <= 64,
+ *          where the FP32 factor stays on chip (registers for n <= 16, one
+ *          warp per matrix with the matrix in shared memory for 17 .. 64),
+ *          and NULL is allowed then
  * Returns 0, or -j: -1 layout -2 uplo -3 n -4 nrhs -6 ldap -8 ldbp -9 V
  * -10 nm -11 max_iter (< 0) -15 lwork (too small). n = 0, nm = 0 or
  * nrhs = 0 return at once, touching nothing. */
@@ -340,15 +342,15 @@ int cbk_cuda_graph_destroy(cbk_cuda_graph graph);
  * It is for callers that cannot allocate device memory at the point of the
  * call: code hosted by a framework or plugin host that owns every device
  * allocation, or a latency-bound loop that must not call cudaMalloc or
- * cudaFree. For n > 16 the FP32 factor needs scratch; here it comes from one
+ * cudaFree. For n > 64 the FP32 factor needs scratch; here it comes from one
  * array of CBK_CUDA_NOALLOC_SCRATCH_BYTES (64 MiB) that the library reserves
- * on every GPU it is used on, for as long as the process runs. n <= 16 needs
+ * on every GPU it is used on, for as long as the process runs. n <= 64 needs
  * none.
  * Arguments, results and return codes are those of
  * cbk_cuda_dposv_refined_compact_async without work and lwork, plus -10 when
  * the batch is too large for the array: when
  * cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) exceeds
- * CBK_CUDA_NOALLOC_SCRATCH_BYTES (for n = 48, about 6,800 matrices; split
+ * CBK_CUDA_NOALLOC_SCRATCH_BYTES (for n = 80, about 2,500 matrices; split
  * larger batches into several calls).
  * The first call on a device looks up the array's device address with that
  * device current: make that first call before any stream capture. Every call

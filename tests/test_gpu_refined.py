@@ -53,11 +53,11 @@ def _plain_factor(A, V, layout="C", uplo="L"):
     return ap.cpu().numpy()
 
 
-@pytest.mark.parametrize("n", [8, 16, 32, 48, 5, 12, 17, 24])
+@pytest.mark.parametrize("n", [8, 16, 32, 48, 5, 12, 17, 24, 33, 40, 56, 64, 65, 70])
 @pytest.mark.parametrize("layout,uplo", [("C", "L"), ("R", "U")])
 def test_refined_meets_fp64_backward_error(n, layout, uplo, cuda):
     rng = np.random.default_rng(1000 + n)
-    nm, nrhs, V = 200, 1 if n % 2 == 0 else 2, 32
+    nm, nrhs, V = (200 if n <= 64 else 70), 1 if n % 2 == 0 else 2, 32
     A, kappa = C.gen_spd_cond(rng, nm, n)
     B = rng.standard_normal((nm, n, nrhs))
     info, X, a1, a0, it, be = _run(A, B, V, layout, uplo)
@@ -119,7 +119,8 @@ def test_refined_argument_checks(cuda):
     f = cbk_gb300.dposv_refined_compact
     assert f("X", "L", 8, 1, None, 8, None, 8, 32, 64) == -1
     assert f("C", "L", 8, 1, None, 8, None, 8, 32, 64, max_iter=-1) == -11
-    assert f("C", "L", 20, 1, None, 20, None, 20, 32, 64, work=0, lwork=0) == -15
+    assert f("C", "L", 70, 1, None, 70, None, 70, 32, 64, work=0, lwork=0) == -15
     assert f("C", "L", 0, 1, None, 1, None, 1, 32, 64) == 0
     assert cbk_gb300.dposv_refined_lwork(8, 1, 32, 64) == 0
-    assert cbk_gb300.dposv_refined_lwork(20, 1, 32, 64) > 20 * 20 * 4 * 64
+    assert cbk_gb300.dposv_refined_lwork(48, 1, 32, 64) == 0  # one warp per matrix, on chip
+    assert cbk_gb300.dposv_refined_lwork(70, 1, 32, 64) > 70 * 70 * 4 * 64

@@ -62,7 +62,7 @@ def _solve_both(n, nm, V, seed):
     return A, B, X_ref, X_na, ref_it.cpu().numpy(), na_it.cpu().numpy()
 
 
-@pytest.mark.parametrize("n,nm", [(48, 4000), (24, 9000), (12, 5000)])
+@pytest.mark.parametrize("n,nm", [(80, 2000), (70, 2900), (48, 4000), (12, 5000)])
 def test_noalloc_matches_workspace_entry_point_twice(n, nm, cuda):
     V = 32
     for call, seed in enumerate((11 * n, 11 * n + 1)):  # two calls in a row, new data each
@@ -76,7 +76,7 @@ def test_noalloc_matches_workspace_entry_point_twice(n, nm, cuda):
 
 def test_noalloc_rejects_a_batch_beyond_its_scratch(cuda):
     import cbk_gb300
-    n, V = 48, 32
+    n, V = 80, 32
     f = _noalloc()
     lw = cbk_gb300.dposv_refined_lwork
     fits = max(nm for nm in range(32, 20000, 32) if lw(n, 1, V, nm) <= SCRATCH)
