@@ -4,30 +4,43 @@
 // The method is cbk_kernels_refine.cu's (FP32 factorization, FP64 refinement,
 // LAPACK dsposv's stopping test, per-matrix FP64 fallback); the mapping and
 // the form of the FP32 solve differ. One thread per matrix cannot hold an FP32
-// factor of order 48 on chip; here the 32 lanes of a warp share one matrix:
+// factor of order 48 on chip; here the 32 lanes of a warp share one matrix.
+// The kernel is compiled for a padded order N (24, 32, .., 64) and a matrix
+// of order n <= N is extended by the identity, so every loop bound and
+// register index is static:
 //   * the block's matrices (consecutive lanes of the compact batch) are staged
-//     once into shared memory as full symmetric FP64 matrices, by all threads
-//     of the block with coalesced loads (odd leading dimension: row and
-//     column sweeps free of bank conflicts);
-//   * lane l holds rows l and l + 32 of the FP32 matrix in registers (the
-//     order's upper bound NMAX is a template parameter, so every register
-//     index is static) and the warp inverts it in place with the symmetric
-//     sweep operator -- Gauss-Jordan elimination without pivoting, stable for
-//     positive-definite matrices (Beaton 1964; Goodnight 1979): pivot k
-//     broadcasts column k through shared memory and every lane updates its
-//     rows, the matrix staying symmetric throughout;
+//     once into shared memory, each as the packed lower triangle of its FP64
+//     matrix (column-major, N (N + 1) / 2 values -- half of a full square, so
+//     twice as many matrices fit on an SM), by all threads of the block with
+//     coalesced loads;
+//   * lane l holds rows l and l + 32 of the FP32 matrix in registers and the
+//     warp inverts it in place with the symmetric sweep operator --
+//     Gauss-Jordan elimination without pivoting, stable for positive-definite
+//     matrices (Beaton 1964; Goodnight 1979): pivot k broadcasts column k
+//     through shared memory and every lane updates its rows. The pivot loop
+//     is not unrolled (its body is one pass over the row); instead every
+//     step rotates the register row by one place as it updates it, so the
+//     pivot column is always register 0;
+//   * the FP32 matrix is the symmetrically scaled D A D, D = diag(2^-h_i) with
+//     h_i = floor(log2(a_ii) / 2): an exact scaling that puts the diagonal in
+//     [1, 4), so every pivot lies in (0, 4) whatever the scale of A, and the
+//     pivot row's update can share the other rows' FMA (coefficient 1/p - 1,
+//     exact or accurate to eps32 for such pivots);
 //   * each FP32 solve is then one matrix-vector product with the inverse --
 //     a lane per row, no serial chain -- where triangular sweeps would be n
 //     dependent shuffle steps each; refinement converges at the same rate
 //     (||I - M A|| ~ kappa eps32);
-//   * the FP64 residual r = b - A x is row-parallel: lane l sweeps its rows of
-//     the staged A with x broadcast from shared memory -- n FMAs per row, the
-//     FP64 pipe's only large load.
+//   * the FP64 residual r = b - A x is row-parallel over the packed FP64
+//     triangle with x broadcast from shared memory: N FMAs per row, the FP64
+//     pipe's only large load. For N <= 48 the rows past 32 are split by
+//     columns over the two half-warps (summed with one shuffle), so no lane
+//     idles in the FP64 pipe.
 // FP64 -> FP32 rounding of A (once per matrix) is done with integer bit
 // operations (round toward zero, subnormals flushed): a hardware conversion
 // takes an FP64-pipe slot on a GB300, and the FP32 inverse only steers the
-// refinement. A non-positive FP32 pivot (not positive definite in FP32) sends
-// the matrix to the FP64 fallback (iters = -1).
+// refinement. An entry beyond the FP32 range sends the matrix to the FP64
+// fallback with iters = -2 (as LAPACK dsposv); a non-positive FP32 pivot
+// (not positive definite in FP32) with iters = -1.
 #include "cbk_device.cuh"
 #include "cbk_launch.h"
 
@@ -42,27 +55,90 @@ namespace {
 constexpr double EPS64 = 2.220446049250313e-16;
 constexpr unsigned FULL = 0xffffffffu;
 
-// FP64 -> FP32 toward zero on the integer pipe; sets *overflow for a finite
-// value beyond the FP32 range (it becomes an infinity).
-__device__ __forceinline__ float d2f_rz(double a, bool &overflow)
+// FP64 -> FP32 toward zero on the integer pipe, times 2^shift (subnormal
+// results flushed, values beyond the FP32 range become infinities).
+__device__ __forceinline__ float d2f_rz(double a, int shift = 0)
 {
     const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
     const unsigned sign = hi & 0x80000000u;
     const int e = (int)((hi >> 20) & 0x7ffu);
     const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const int fe = e - 1023 + 127;
+    const int fe = e - 1023 + 127 + shift;
     unsigned bits;
     if (e == 0x7ff)
         bits = sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u | mant : 0u);
-    else if (fe >= 255) {
-        bits = sign | 0x7f800000u;
-        overflow = true;
-    }
-    else if (fe <= 0)
+    else if (e == 0 || fe <= 0)
         bits = sign;
+    else if (fe >= 255)
+        bits = sign | 0x7f800000u;
     else
         bits = sign | ((unsigned)fe << 23) | mant;
     return __uint_as_float(bits);
+}
+
+// The same for |a| < 2^128 (callers check the range apart): no branches.
+// Zeros, FP64 subnormals and results below the FP32 normal range give a
+// signed zero; a NaN gives some float (its residual stays NaN).
+__device__ __forceinline__ float d2f_rz_inrange(double a)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const int fe = (int)((hi >> 20) & 0x7ffu) - 896;
+    const unsigned bits =
+        (hi & 0x80000000u) | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(fe > 0 ? bits : hi & 0x80000000u);
+}
+
+// FP32 -> FP64 times 2^shift on the integer pipe (exact; FP32 subnormals
+// flushed to zero)
+__device__ __forceinline__ double f2d_int(float f, int shift = 0)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u;
+    const int e = (int)((u >> 23) & 0xffu);
+    const unsigned mant = u & 0x7fffffu;
+    unsigned hi;
+    if (e == 0)
+        return __hiloint2double((int)sign, 0);
+    if (e == 0xff)
+        hi = sign | 0x7ff00000u | (mant >> 3) | (mant ? 0x80000u : 0u);
+    else
+        hi = sign | ((unsigned)(e - 127 + 1023 + shift) << 20) | (mant >> 3);
+    return __hiloint2double((int)hi, (int)(mant << 29));
+}
+
+// 1/p from the SFU's approximate reciprocal (relative error below 2^-22):
+// the FP32 inverse only steers the refinement
+__device__ __forceinline__ float rcp_approx(float p)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(p));
+    return r;
+}
+
+// |a| > FLT_MAX, infinities included and NaN not (LAPACK dlag2s's test), on
+// the 32-bit halves of a
+__device__ __forceinline__ bool beyond_fp32(double a)
+{
+    const unsigned ah = (unsigned)__double2hiint(a) & 0x7fffffffu, lo = (unsigned)__double2loint(a);
+    const bool big = ah > 0x47efffffu || (ah == 0x47efffffu && lo > 0xe0000000u);
+    const bool nan = ah > 0x7ff00000u || (ah == 0x7ff00000u && lo != 0u);
+    return big && !nan;
+}
+
+// floor(e / 2) for a = m 2^e > 0 (m in [1, 2)), clamped to [-63, 63); 0 for a
+// diagonal that is not a positive normal number (the pivot test catches it)
+__device__ __forceinline__ int half_exp(double a)
+{
+    const int hi = __double2hiint(a);
+    const int eb = (hi >> 20) & 0x7ff;
+    if (hi < 0 || eb == 0 || eb == 0x7ff) return 0;
+    return min(max((eb - 1023) >> 1, -63), 63);
+}
+
+// 2^k as a float, |k| <= 126
+__device__ __forceinline__ float exp2i(int k)
+{
+    return __int_as_float((127 + k) << 23);
 }
 
 __device__ __forceinline__ float warp_max(float v)
@@ -71,6 +147,26 @@ __device__ __forceinline__ float warp_max(float v)
     for (int o = 16; o > 0; o >>= 1)
         v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
     return v;
+}
+
+// the packed lower triangle of an order-N matrix, column-major: column j
+// starts at pk_col(N, j) and element (i, j), i >= j, is at pk_col(N, j) + i - j
+__host__ __device__ constexpr int pk_col(int N, int j)
+{
+    return j * (2 * N - j + 1) / 2;
+}
+
+// doubles per staged matrix: the triangle, padded to 8 (mod 16) doubles so
+// that the block's matrices start in alternate halves of the 32 banks
+__host__ __device__ constexpr int pk_stride(int N)
+{
+    return N * (N + 1) / 2 + ((8 - (N * (N + 1) / 2) % 16) + 16) % 16;
+}
+
+template <int N, int WPB> constexpr size_t warp_smem_bytes()
+{
+    return (size_t)WPB * ((size_t)pk_stride(N) * sizeof(double) + (size_t)N * sizeof(double) +
+                          (size_t)3 * N * sizeof(float));
 }
 
 struct WarpOut {
@@ -94,83 +190,156 @@ __device__ __forceinline__ void warp_fallback(int n, int nrhs, int first, LV<dou
     }
 }
 
-// d (this lane's rows) := -M z, M = -A32^-1 held as register rows: z is
-// broadcast from shared memory (SR, this warp's n floats).
-template <int NMAX>
-__device__ __forceinline__ void apply_inverse(int n, int lane, const float (&Mr)[(NMAX + 31) / 32][NMAX],
-                                              float *SR, float (&z)[(NMAX + 31) / 32])
+// Where the FP32 matrix lives. R0 is row `lane` (all N columns, zero for a
+// lane past N). R1 is the second row part: none for N <= 32 (one unused
+// register), row lane + 32 for N > 48, and for 32 < N <= 48 half of row
+// 32 + lane % 16 -- columns [0, N/2) in lanes 0..15, [N/2, N) in lanes
+// 16..31 -- so that no lane carries an empty row through the sweep.
+template <int N> struct Rows {
+    static constexpr bool TWO = N > 32;
+    static constexpr bool SPLIT = TWO && N <= 48;
+    static constexpr int H = N / 2;
+    static constexpr int W1 = !TWO ? 1 : (SPLIT ? H : N);
+};
+
+// z := -M z for this lane's rows, with M = -(D A D)^-1 in R0 / R1 and z
+// broadcast through shared memory (SR, this warp's N floats): given z = D v,
+// D z is then A32^-1 v. Row lane + 32 r is z[r] (lanes 0..15 for r = 1 when
+// the second rows are split). Two partial sums per row break the FMA chain.
+template <int N>
+__device__ __forceinline__ void apply_inverse(int lane, const float (&R0)[N],
+                                              const float (&R1)[Rows<N>::W1], float *SR,
+                                              float (&z)[(N + 31) / 32])
 {
-    constexpr int NR = (NMAX + 31) / 32;
+    using L = Rows<N>;
+    constexpr int NR = (N + 31) / 32;
     __syncwarp();
 #pragma unroll
     for (int r = 0; r < NR; ++r)
-        if (lane + 32 * r < n) SR[lane + 32 * r] = z[r];
+        if (lane + 32 * r < N) SR[lane + 32 * r] = z[r];
     __syncwarp();
-    float acc[NR];
+    float a0[2] = {0.f, 0.f}, a1[2] = {0.f, 0.f};
+    if constexpr (L::SPLIT) {
+        const bool lower = lane < 16;
 #pragma unroll
-    for (int r = 0; r < NR; ++r)
-        acc[r] = 0.f;
-#pragma unroll
-    for (int j = 0; j < NMAX; ++j) {
-        if (j >= n) break;
-        const float zj = SR[j];
-#pragma unroll
-        for (int r = 0; r < NR; ++r)
-            acc[r] = fmaf(Mr[r][j], zj, acc[r]);
+        for (int t = 0; t < L::H; ++t) {
+            const float za = SR[t], zb = SR[t + L::H];
+            a0[t & 1] = fmaf(R0[t], za, a0[t & 1]);
+            a0[t & 1] = fmaf(R0[t + L::H], zb, a0[t & 1]);
+            a1[t & 1] = fmaf(R1[t], lower ? za : zb, a1[t & 1]);
+        }
+        float b = a1[0] + a1[1];
+        b += __shfl_xor_sync(FULL, b, 16);
+        z[0] = -(a0[0] + a0[1]);
+        z[1] = -b;
     }
+    else {
 #pragma unroll
-    for (int r = 0; r < NR; ++r)
-        z[r] = -acc[r];
+        for (int j = 0; j < N; ++j) {
+            const float zj = SR[j];
+            a0[j & 1] = fmaf(R0[j], zj, a0[j & 1]);
+            if constexpr (L::TWO) a1[j & 1] = fmaf(R1[j], zj, a1[j & 1]);
+        }
+        z[0] = -(a0[0] + a0[1]);
+        if constexpr (L::TWO) z[NR - 1] = -(a1[0] + a1[1]);
+    }
 }
 
-template <int NMAX, int WPB>
-__global__ void __launch_bounds__(WPB * 32)
+// acc[r] := b[r] - (A x)(row lane + 32 r) from the packed FP64 triangle SA and
+// x in SX. Rows 32 .. N-1 of an order N <= 48 go to both half-warps, lane l
+// summing columns [0, N/2) (l < 16) or [N/2, N) (l >= 16) of row 32 + l % 16.
+template <int N>
+__device__ __forceinline__ void residual(int lane, const double *SA, const double *SX,
+                                         const double (&b)[(N + 31) / 32],
+                                         double (&acc)[(N + 31) / 32])
+{
+    constexpr int NR = (N + 31) / 32;
+    {
+        const int i = min(lane, N - 1); // lanes past N (N < 32) compute a row they discard
+        const int ci = pk_col(N, i) - i;
+        double s = b[0];
+#pragma unroll 4
+        for (int j = 0; j < N; ++j)
+            s = fma(-SA[j <= i ? pk_col(N, j) - j + i : ci + j], SX[j], s);
+        acc[0] = s;
+    }
+    if constexpr (NR == 2) {
+        if constexpr (N <= 48) {
+            constexpr int H = N / 2;
+            static_assert(N % 2 == 0, "split rows need an even order");
+            const bool lo = lane < 16;
+            const int i = min(32 + (lane & 15), N - 1);
+            const int ci = pk_col(N, i) - i;
+            const int c0 = lo ? 0 : H;
+            double s = lo ? b[1] : 0.0;
+#pragma unroll 4
+            for (int t = 0; t < H; ++t) {
+                // the first half's columns all lie left of the row (t < H <= 32 <= i)
+                const int j = c0 + t;
+                const int off = lo ? pk_col(N, t) - t + i
+                                   : (H + t <= i ? pk_col(N, H + t) - (H + t) + i : ci + j);
+                s = fma(-SA[off], SX[j], s);
+            }
+            acc[1] = s + __shfl_xor_sync(FULL, s, 16);
+        }
+        else {
+            const int i = min(lane + 32, N - 1);
+            const int ci = pk_col(N, i) - i;
+            double s = b[1];
+#pragma unroll 4
+            for (int j = 0; j < N; ++j)
+                s = fma(-SA[j <= i ? pk_col(N, j) - j + i : ci + j], SX[j], s);
+            acc[1] = s;
+        }
+    }
+}
+
+template <int N, int WPB, int MINB>
+__global__ void __launch_bounds__(WPB * 32, MINB)
     k_posv_refined_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
                         int ldbp, int V, long nlanes, size_t sa, size_t sb, WarpOut out)
 {
-    constexpr int NR = (NMAX + 31) / 32;
+    constexpr int NR = (N + 31) / 32;
+    constexpr int PKS = pk_stride(N);
+    static_assert(N % 8 == 0 && N >= 24 && N <= 64, "padded order");
     extern __shared__ __align__(16) unsigned char smem[];
+    double *const SAall = reinterpret_cast<double *>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long m0 = (long)blockIdx.x * WPB;
     const long m = m0 + warp;
-    const int lds = n | 1; // odd: row and column sweeps free of bank conflicts
-    const int nx = (n + 1) & ~1, nc = (n + 3) & ~3; // vector lengths padded for 16-byte loads
-    double *SAall = reinterpret_cast<double *>(smem);
-    double *SA = SAall + (size_t)warp * n * lds;
-    double *SX = SAall + (((size_t)WPB * n * lds + 1) & ~(size_t)1) + (size_t)warp * nx;
-    float *SC = reinterpret_cast<float *>(SAall + (((size_t)WPB * n * lds + 1) & ~(size_t)1) +
-                                          (size_t)WPB * nx) +
-                (size_t)warp * 2 * nc;
-    float *SR = SC + nc;
+    double *const SA = SAall + warp * PKS;
+    double *const SX = SAall + WPB * PKS + warp * N;
+    // the pivot column twice over (SC, 16-byte aligned: N is a multiple of 8)
+    // and the vector of a matrix-vector product (SR)
+    float *const SC = reinterpret_cast<float *>(SAall + WPB * (PKS + N)) + warp * 3 * N;
+    float *const SR = SC + 2 * N;
 
-    // ---- stage A (the lower triangle of each matrix's view, mirrored) ----
+    // ---- stage the block's matrices: packed lower triangles, identity past n ----
+    // thread t copies matrix t % WPB, rows t / WPB + 32 s of each column:
+    // a warp's loads cover WPB neighbouring lanes of eight rows (whole
+    // 32-byte sectors), and its stores two wavefronts
     {
-        long gw[WPB];
-        int vw[WPB];
+        LV<double> A0 = lv_make<double>(ap, row, ldap, V);
+        if (up) A0 = A0.t();
+        const int w = threadIdx.x % WPB, rr = threadIdx.x / WPB;
+        const bool have = m0 + w < nlanes;
+        const long mw = have ? m0 + w : nlanes - 1;
+        const long gw = mw / V;
+        const double *bw = ap + gw * sa + (mw - gw * V);
+        double *Sw = SAall + w * PKS;
+#pragma unroll 1
+        for (int j = 0; j < N; ++j) {
+            const double *colp = bw + (long)j * A0.sj;
+            double *Sj = Sw + pk_col(N, j) - j;
+            const bool jn = have && j < n;
 #pragma unroll
-        for (int w = 0; w < WPB; ++w) {
-            gw[w] = (m0 + w) / V;
-            vw[w] = (int)(m0 + w - gw[w] * V);
-        }
-        for (int j = 0; j < n; ++j) {
-            const int cnt = (n - j) * WPB;
-            for (int p = threadIdx.x; p < cnt; p += WPB * 32) {
-                const int w = p % WPB, i = j + p / WPB;
-                if (m0 + w >= nlanes) continue;
-                long g = 0;
-                int v = 0;
-#pragma unroll
-                for (int q = 0; q < WPB; ++q)
-                    if (q == w) {
-                        g = gw[q];
-                        v = vw[q];
-                    }
-                LV<double> A = lv_make<double>(ap + g * sa + v, row, ldap, V);
-                if (up) A = A.t();
-                const double a = A(i, j);
-                double *S = SAall + (size_t)w * n * lds;
-                S[(size_t)j * lds + i] = a;
-                S[(size_t)i * lds + j] = a;
+            for (int s = 0; s < (N + 31) / 32; ++s) {
+                const int i = j + rr + 32 * s;
+                if (i < N) {
+                    double a = (i == j) ? 1.0 : 0.0;
+                    if (jn && i < n) a = colp[(long)i * A0.si];
+                    Sj[i] = a;
+                }
             }
         }
     }
@@ -182,114 +351,268 @@ __global__ void __launch_bounds__(WPB * 32)
     if (up) Ag = Ag.t();
     const LV<double> B = lv_make<double>(bp + g * sb + v, row, ldbp, V);
 
-    // ---- FP32 rows (both triangles) in registers, ||A||_inf ----
-    float Mr[NR][NMAX];
-    bool ovf = false;
-    float rs = 0.f;
+    // ---- the scaling D and the FP32 rows of D A D; ||A||_inf of the n rows ----
+    int h[NR]; // D(i, i) = 2^-h
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
         const int i = lane + 32 * r;
-        float s = 0.f;
-#pragma unroll
-        for (int j = 0; j < NMAX; ++j) {
-            float f = 0.f;
-            if (i < n && j < n) {
-                f = d2f_rz(SA[(size_t)j * lds + i], ovf);
-                s += fabsf(f);
-            }
-            Mr[r][j] = f;
+        h[r] = 0;
+        if (i < N) {
+            h[r] = half_exp(SA[pk_col(N, i)]);
+            SR[i] = exp2i(-h[r]);
         }
-        rs = fmaxf(rs, s);
+    }
+    __syncwarp();
+    using L = Rows<N>;
+    constexpr int H = L::H;
+    float R0[N], R1[L::W1];
+    unsigned hmax = 0; // largest high word of |a| read: a quick screen for the FP32 range
+    float rs = 0.f;
+    {
+        const int i = min(lane, N - 1);
+        const int ci = pk_col(N, i) - i;
+        const bool real = N >= 32 || lane < N;
+        const float di = exp2i(-h[0]);
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const double a = SA[j <= i ? pk_col(N, j) - j + i : ci + j];
+            hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
+            const float f = d2f_rz_inrange(a);
+            sum += fabsf(f);
+            R0[j] = real ? f * (di * SR[j]) : 0.f;
+        }
+        if (lane < n) rs = sum;
+    }
+    if constexpr (!L::TWO) {
+        R1[0] = 0.f;
+    }
+    else if constexpr (L::SPLIT) {
+        const bool lower = lane < 16;
+        const int ib = 32 + (lane & 15);
+        const int i = min(ib, N - 1);
+        const int ci = pk_col(N, i) - i;
+        const bool real = N >= 48 || ib < N;
+        const float di = SR[i];
+        float sum = 0.f;
+#pragma unroll
+        for (int t = 0; t < H; ++t) {
+            const int j = (lower ? 0 : H) + t;
+            const int off = lower ? pk_col(N, t) - t + i
+                                  : (H + t <= i ? pk_col(N, H + t) - (H + t) + i : ci + j);
+            const double a = SA[off];
+            hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
+            const float f = d2f_rz_inrange(a);
+            sum += fabsf(f);
+            R1[t] = real ? f * (di * SR[j]) : 0.f;
+        }
+        sum += __shfl_xor_sync(FULL, sum, 16);
+        if (ib < n) rs = fmaxf(rs, sum);
+    }
+    else {
+        const int i = min(lane + 32, N - 1);
+        const int ci = pk_col(N, i) - i;
+        const bool real = lane + 32 < N;
+        const float di = exp2i(-h[1]);
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const double a = SA[j <= i ? pk_col(N, j) - j + i : ci + j];
+            hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
+            const float f = d2f_rz_inrange(a);
+            sum += fabsf(f);
+            R1[j] = real ? f * (di * SR[j]) : 0.f;
+        }
+        if (lane + 32 < n) rs = fmaxf(rs, sum);
     }
     const float anorm = warp_max(rs);
-    int status = __any_sync(FULL, ovf) ? -2 : 0;
+    int status = 0;
+    if (__any_sync(FULL, hmax >= 0x47efffffu)) {
+        // an entry at or near the FP32 limit: the exact test, on the rare path
+        bool ovf = false;
+        for (int e = lane; e < pk_col(N, N); e += 32)
+            ovf |= beyond_fp32(SA[e]);
+        if (__any_sync(FULL, ovf)) status = -2;
+    }
 
-    // ---- FP32 inverse by the symmetric sweep: after all n pivots Mr = -A^-1 ----
+    // ---- FP32 inverse by the symmetric sweep: after all N pivots M = -(D A D)^-1 ----
     // pivot k, with c = column k (= row k) and p = c_k:
     //   rows i != k:  M(i,j) -= (c_i / p) c_j  (j != k),  M(i,k) = c_i / p
     //   row k:        M(k,j)  = c_j / p        (j != k),  M(k,k) = -1 / p
     // the row-k case is the same FMA with the coefficient 1/p - 1 (its row
-    // equals c before the pivot), so every lane runs one instruction stream
+    // equals c before the pivot), so every lane runs one instruction stream.
+    // The pivots go in groups of U = 8: at the start of the group of pivots
+    // k0 .. k0+7, register q of a row holds column (k0 + q) mod N, so within
+    // the group every register index is static; the group ends by rotating
+    // the registers by 8 (a split row passes 8 values across with shuffles).
+    constexpr int U = 8;
+    static_assert(N % U == 0 && H % 4 == 0, "pivot groups and float4 columns");
+    bool nonpos = false;
+#pragma unroll 1
+    for (int k0 = 0; k0 < N; k0 += U) {
+        // c[q] = column (k0 + q) mod N from the doubled column; the upper half
+        // of a split row reads from c[H] on
+        const float4 *C4 = reinterpret_cast<const float4 *>(SC + k0);
+        const float4 *CB4 =
+            reinterpret_cast<const float4 *>(SC + k0 + ((L::SPLIT && lane >= 16) ? H : 0));
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k) {
-        if (k >= n) break;
-        __syncwarp();
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u;
+            __syncwarp();
+            if (N >= 32 || lane < N) {
+                SC[lane] = R0[u];
+                SC[lane + N] = R0[u];
+            }
+            if constexpr (L::TWO) {
+                if ((!L::SPLIT || lane < 16) && 32 + lane < N) {
+                    SC[32 + lane] = R1[u];
+                    SC[32 + lane + N] = R1[u];
+                }
+            }
+            __syncwarp();
+            const float p = SC[k];
+            nonpos |= !(p > 0.f);
+            const float rp = rcp_approx(p);
+            const bool own0 = lane == k;
+            const float w0 = R0[u] * rp;
+            const float beta0 = own0 ? rp - 1.0f : -w0;
+            const float last0 = own0 ? -rp : w0;
+            float betab = 0.f, lastb = 0.f;
+            if constexpr (L::TWO) {
+                float vb = R1[u];
+                if constexpr (L::SPLIT) {
+                    const float o = __shfl_xor_sync(FULL, R1[u], 16);
+                    vb = lane < 16 ? R1[u] : o; // column k of row 32 + lane % 16
+                }
+                const bool ownb = (L::SPLIT ? 32 + (lane & 15) : 32 + lane) == k;
+                const float wb = vb * rp;
+                betab = ownb ? rp - 1.0f : -wb;
+                lastb = ownb ? -rp : wb;
+            }
 #pragma unroll
-        for (int r = 0; r < NR; ++r)
-            if (lane + 32 * r < n) SC[lane + 32 * r] = Mr[r][k];
-        __syncwarp();
-        const float p = SC[k];
-        if (!(p > 0.f) && status == 0) status = -1;
-        const float rp = 1.0f / p;
-        float beta[NR];
+            for (int q4 = 0; q4 < N / 4; ++q4) {
+                const float4 c4 = C4[q4];
+                const float cq[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-        for (int r = 0; r < NR; ++r) {
-            const bool own = (lane + 32 * r == k);
-            const float wi = Mr[r][k] * rp;
-            beta[r] = own ? rp - 1.0f : -wi;
-            Mr[r][k] = own ? -rp : wi;
+                for (int e = 0; e < 4; ++e) {
+                    const int q = 4 * q4 + e;
+                    if (q != u) {
+                        R0[q] = fmaf(beta0, cq[e], R0[q]);
+                        if constexpr (L::TWO && !L::SPLIT) R1[q] = fmaf(betab, cq[e], R1[q]);
+                    }
+                }
+            }
+            R0[u] = last0;
+            if constexpr (L::TWO && !L::SPLIT) R1[u] = lastb;
+            if constexpr (L::SPLIT) {
+#pragma unroll
+                for (int t4 = 0; t4 < H / 4; ++t4) {
+                    const float4 c4 = CB4[t4];
+                    const float cq[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int t = 4 * t4 + e;
+                        const float nv = fmaf(betab, cq[e], R1[t]);
+                        // the pivot column sits in the lower half (u < 8 <= H)
+                        R1[t] = (t == u && lane < 16) ? lastb : nv;
+                    }
+                }
+            }
         }
+        // rotate by U: register q takes column k0 + U + q
+        {
+            float t0[U];
 #pragma unroll
-        for (int j = 0; j < NMAX; ++j) {
-            if (j >= n) break;
-            if (j == k) continue;
-            const float cj = SC[j];
+            for (int e = 0; e < U; ++e)
+                t0[e] = R0[e];
 #pragma unroll
-            for (int r = 0; r < NR; ++r)
-                Mr[r][j] = fmaf(beta[r], cj, Mr[r][j]);
+            for (int q = 0; q < N - U; ++q)
+                R0[q] = R0[q + U];
+#pragma unroll
+            for (int e = 0; e < U; ++e)
+                R0[N - U + e] = t0[e];
+        }
+        if constexpr (L::TWO && !L::SPLIT) {
+            float t1[U];
+#pragma unroll
+            for (int e = 0; e < U; ++e)
+                t1[e] = R1[e];
+#pragma unroll
+            for (int q = 0; q < N - U; ++q)
+                R1[q] = R1[q + U];
+#pragma unroll
+            for (int e = 0; e < U; ++e)
+                R1[N - U + e] = t1[e];
+        }
+        if constexpr (L::SPLIT) {
+            // lower half: V[t] = V[t + 8], the last 8 from the upper half's
+            // first 8; upper half: the same, the last 8 from the lower half's
+            float t1[U];
+#pragma unroll
+            for (int e = 0; e < U; ++e)
+                t1[e] = __shfl_xor_sync(FULL, R1[e], 16);
+#pragma unroll
+            for (int t = 0; t < H - U; ++t)
+                R1[t] = R1[t + U];
+#pragma unroll
+            for (int e = 0; e < U; ++e)
+                R1[H - U + e] = t1[e];
         }
     }
+    if (nonpos && status == 0) status = -1;
 
+    // LAPACK dsposv's test ||r|| <= sqrt(n) eps64 ||A|| ||x||, in FP32 while
+    // the right side is a normal FP32 number, in FP64 below that
     const double cte = (double)anorm * EPS64 * sqrt((double)n);
+    const float cte32 = (float)cte;
     int it_max = 0, col = 0;
     float worst = 0.f;
     for (; col < nrhs && status == 0; ++col) {
+        // all FP64 <-> FP32 conversions here are integer operations; w holds
+        // D b and then D r (the scaling folded into the exponent). x lives in
+        // SX and b is re-read from B: registers are kept for the FP32 rows.
         float w[NR];
-        double b64[NR], x[NR];
         float bn = 0.f;
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             const int i = lane + 32 * r;
-            b64[r] = (i < n) ? B(i, col) : 0.0;
-            w[r] = (float)b64[r];
-            bn = fmaxf(bn, fabsf(w[r]));
+            const double b = (i < n) ? B(i, col) : 0.0;
+            bn = fmaxf(bn, fabsf(d2f_rz(b)));
+            w[r] = d2f_rz(b, -h[r]);
         }
         bn = warp_max(bn);
-        apply_inverse<NMAX>(n, lane, Mr, SR, w);
+        apply_inverse<N>(lane, R0, R1, SR, w);
         float xn = 0.f;
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
-            x[r] = (lane + 32 * r < n) ? (double)w[r] : 0.0;
-            xn = fmaxf(xn, fabsf(w[r]));
+            const int i = lane + 32 * r;
+            const double x = (i < n) ? f2d_int(w[r], -h[r]) : 0.0;
+            xn = fmaxf(xn, fabsf(d2f_rz(x)));
+            if (i < N) SX[i] = x;
         }
         xn = warp_max(xn);
         float rprev = INFINITY;
         for (int it = 0;; ++it) {
             __syncwarp();
-#pragma unroll
-            for (int r = 0; r < NR; ++r)
-                if (lane + 32 * r < n) SX[lane + 32 * r] = x[r];
-            __syncwarp();
-            // r = b - A x, lane-parallel over rows, x broadcast from shared
             double acc[NR];
 #pragma unroll
             for (int r = 0; r < NR; ++r)
-                acc[r] = b64[r];
-            for (int j = 0; j < n; ++j) {
-                const double xj = SX[j];
-                const double *Sj = SA + (size_t)j * lds + lane;
-#pragma unroll
-                for (int r = 0; r < NR; ++r)
-                    if (lane + 32 * r < n) acc[r] = fma(-Sj[32 * r], xj, acc[r]);
-            }
+                acc[r] = (lane + 32 * r < n) ? B(lane + 32 * r, col) : 0.0;
+            residual<N>(lane, SA, SX, acc, acc);
             float rn = 0.f;
+            bool nan = false; // fmaxf drops a NaN: a NaN residual must stop the refinement
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
-                w[r] = (lane + 32 * r < n) ? (float)acc[r] : 0.f;
-                rn = fmaxf(rn, fabsf(w[r]));
+                const bool real = lane + 32 * r < n;
+                const float v = real ? fabsf(d2f_rz(acc[r])) : 0.f;
+                nan |= v != v;
+                rn = fmaxf(rn, v);
+                w[r] = real ? d2f_rz(acc[r], -h[r]) : 0.f;
             }
-            rn = warp_max(rn);
-            if ((double)rn <= cte * (double)xn) {
+            rn = __any_sync(FULL, nan) ? NAN : warp_max(rn);
+            const float thr = cte32 * xn;
+            const bool done = thr >= 0x1p-100f ? rn <= thr : (double)rn <= cte * (double)xn;
+            if (done) {
                 const float den = anorm * xn + bn;
                 worst = fmaxf(worst, den > 0.f ? rn / den : 0.f);
                 it_max = max(it_max, it);
@@ -300,19 +623,24 @@ __global__ void __launch_bounds__(WPB * 32)
                 break;
             }
             rprev = rn;
-            apply_inverse<NMAX>(n, lane, Mr, SR, w);
+            apply_inverse<N>(lane, R0, R1, SR, w); // syncs the warp: SX reads are done
             float xm = 0.f;
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
-                if (lane + 32 * r < n) x[r] += (double)w[r];
-                xm = fmaxf(xm, fabsf((float)x[r]));
+                const int i = lane + 32 * r;
+                if (i < n) {
+                    const double x = SX[i] + f2d_int(w[r], -h[r]);
+                    SX[i] = x;
+                    xm = fmaxf(xm, fabsf(d2f_rz(x)));
+                }
             }
             xn = warp_max(xm);
         }
         if (status == 0) {
+            __syncwarp();
 #pragma unroll
             for (int r = 0; r < NR; ++r)
-                if (lane + 32 * r < n) B(lane + 32 * r, col) = x[r];
+                if (lane + 32 * r < n) B(lane + 32 * r, col) = SX[lane + 32 * r];
         }
     }
     if (status != 0 && lane == 0) warp_fallback(n, nrhs, status == -3 ? col - 1 : 0, Ag, B);
@@ -322,20 +650,21 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 }
 
-template <int NMAX, int WPB>
+template <int N, int WPB, int MINB>
 cudaError_t launch_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
                         int ldbp, int V, int nm, const WarpOut &out, cudaStream_t s)
 {
     const long ng = ((long)nm + V - 1) / V;
     const long nlanes = ng * V;
-    const size_t nx = (n + 1) & ~1, nc = (n + 3) & ~3;
-    const size_t smem = (((size_t)WPB * n * (n | 1) + 1) & ~(size_t)1) * sizeof(double) +
-                        (size_t)WPB * nx * sizeof(double) + (size_t)WPB * 2 * nc * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_posv_refined_warp<NMAX, WPB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    constexpr size_t smem = warp_smem_bytes<N, WPB>();
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k_posv_refined_warp<N, WPB, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     const unsigned blocks = (unsigned)((nlanes + WPB - 1) / WPB);
-    k_posv_refined_warp<NMAX, WPB><<<blocks, WPB * 32, smem, s>>>(
+    k_posv_refined_warp<N, WPB, MINB><<<blocks, WPB * 32, smem, s>>>(
         row, up, n, nrhs, ap, ldap, bp, ldbp, V, nlanes, gstride(row, ldap, n, n, V),
         gstride(row, ldbp, n, nrhs, V), out);
     return cudaGetLastError();
@@ -354,11 +683,23 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
                                      int *iters, double *berr, cudaStream_t s)
 {
     const WarpOut out{iters, berr, nm, max_iter};
-    // four matrices per block: the staging loads then use whole 32-byte
-    // sectors of the compact layout (four FP64 lanes)
-    if (n <= 32) return launch_warp<32, 4>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s);
-    if (n <= 48) return launch_warp<48, 4>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s);
-    return launch_warp<64, 4>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s);
+    // four matrices per block (the staging loads then fill 32-byte sectors);
+    // the order is padded to a multiple of 8, and the last template argument
+    // caps the registers for the resident blocks wanted. Variant 1 caps them
+    // one block lower (more registers per thread).
+    const bool roomy = variant_for(R_POSV_REFINED, n, 8) == 1;
+#define CBK_WARP(N, B)                                                                             \
+    return roomy ? launch_warp<N, 4, B - 1>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s)   \
+                 : launch_warp<N, 4, B>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s)
+    switch ((n + 7) / 8) {
+    case 3: CBK_WARP(24, 6);
+    case 4: CBK_WARP(32, 5);
+    case 5: CBK_WARP(40, 4);
+    case 6: CBK_WARP(48, 4);
+    case 7: CBK_WARP(56, 3);
+    default: CBK_WARP(64, 3);
+    }
+#undef CBK_WARP
 }
 
 } // namespace cbkcuda

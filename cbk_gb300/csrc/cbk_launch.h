@@ -14,6 +14,12 @@ namespace cbkcuda {
 // Threads per block of the lane-per-matrix kernels (the autotuner may change
 // it per routine and order; 0 selects the built-in default).
 int threads_for(int routine, int n, int dsize);
+void set_threads(int routine, int n, int dsize, int threads);
+
+// Compiled shape of a kernel that has several (0 = the built-in default).
+constexpr int MAX_VARIANTS = 2;
+int variant_for(int routine, int n, int dsize);
+void set_variant(int routine, int n, int dsize, int variant);
 
 enum Routine {
     R_POTRF = 0, R_SYTRFNP, R_POTRS, R_POSV, R_SYTRSNP, R_SYSVNP, R_TRSM, R_GEQRF, R_ORMQR,

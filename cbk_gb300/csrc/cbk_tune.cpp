@@ -1,9 +1,13 @@
-// cbk_tune.cpp -- launch-shape table of the lane-per-matrix kernels.
+// cbk_tune.cpp -- launch-shape table of the kernels.
 //
-// threads_for(routine, n, dsize) gives the threads per block for a routine at
-// order n and scalar size dsize. The defaults come from the table below; the
-// autotuner (cbk_cuda_autotune, cbk_autotune.cu) overwrites entries with
-// measured winners, and CBK_CUDA_THREADS=<t> forces one value everywhere.
+// threads_for(routine, n, dsize) gives the threads per block of a
+// lane-per-matrix kernel for a routine at order n and scalar size dsize;
+// variant_for(...) picks between a kernel's compiled shapes where it has more
+// than one (for the warp-per-matrix refined solve: registers per thread
+// against resident blocks). Both default to the built-in choice (0); the
+// autotuner (cbk_cuda_autotune, cbk_autotune.cpp) overwrites entries with
+// measured winners, and CBK_CUDA_THREADS=<t> / CBK_CUDA_VARIANT=<v> force one
+// value everywhere.
 #include "cbk_launch.h"
 
 #include <atomic>
@@ -15,7 +19,9 @@ namespace {
 
 constexpr int NMAX = 65; // orders 0..64 tuned individually, larger share slot 64
 std::atomic<int> g_table[R_COUNT][2][NMAX];
+std::atomic<int> g_variant[R_COUNT][2][NMAX];
 std::atomic<int> g_forced{-1};
+std::atomic<int> g_forced_variant{-2};
 
 int forced()
 {
@@ -30,12 +36,30 @@ int forced()
     return f;
 }
 
+int forced_variant()
+{
+    int f = g_forced_variant.load(std::memory_order_relaxed);
+    if (f < -1) {
+        const char *e = std::getenv("CBK_CUDA_VARIANT");
+        int v = e ? std::atoi(e) : -1;
+        if (v < 0 || v >= MAX_VARIANTS) v = -1;
+        g_forced_variant.store(v, std::memory_order_relaxed);
+        f = v;
+    }
+    return f;
+}
+
+int slot_of(int n)
+{
+    return n < 0 ? 0 : (n >= NMAX ? NMAX - 1 : n);
+}
+
 } // namespace
 
 int threads_for(int routine, int n, int dsize)
 {
     if (int f = forced()) return f;
-    const int slot = n < 0 ? 0 : (n >= NMAX ? NMAX - 1 : n);
+    const int slot = slot_of(n);
     const int t = (routine >= 0 && routine < R_COUNT)
                       ? g_table[routine][dsize == 8 ? 1 : 0][slot].load(std::memory_order_relaxed)
                       : 0;
@@ -45,8 +69,21 @@ int threads_for(int routine, int n, int dsize)
 void set_threads(int routine, int n, int dsize, int threads)
 {
     if (routine < 0 || routine >= R_COUNT) return;
-    const int slot = n < 0 ? 0 : (n >= NMAX ? NMAX - 1 : n);
-    g_table[routine][dsize == 8 ? 1 : 0][slot].store(threads, std::memory_order_relaxed);
+    g_table[routine][dsize == 8 ? 1 : 0][slot_of(n)].store(threads, std::memory_order_relaxed);
+}
+
+int variant_for(int routine, int n, int dsize)
+{
+    const int f = forced_variant();
+    if (f >= 0) return f;
+    if (routine < 0 || routine >= R_COUNT) return 0;
+    return g_variant[routine][dsize == 8 ? 1 : 0][slot_of(n)].load(std::memory_order_relaxed);
+}
+
+void set_variant(int routine, int n, int dsize, int variant)
+{
+    if (routine < 0 || routine >= R_COUNT || variant < 0 || variant >= MAX_VARIANTS) return;
+    g_variant[routine][dsize == 8 ? 1 : 0][slot_of(n)].store(variant, std::memory_order_relaxed);
 }
 
 } // namespace cbkcuda
