@@ -141,6 +141,19 @@ __device__ __forceinline__ float exp2i(int k)
     return __int_as_float((127 + k) << 23);
 }
 
+// 8-byte asynchronous copy global -> shared (cp.async, cached in L1 and L2)
+__device__ __forceinline__ void cp_async8(double *dst, const double *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+// wait for every cp.async this thread issued
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 __device__ __forceinline__ float warp_max(float v)
 {
 #pragma unroll
@@ -165,7 +178,7 @@ __host__ __device__ constexpr int pk_stride(int N)
 
 template <int N, int WPB> constexpr size_t warp_smem_bytes()
 {
-    return (size_t)WPB * ((size_t)pk_stride(N) * sizeof(double) + (size_t)N * sizeof(double) +
+    return (size_t)WPB * ((size_t)pk_stride(N) * sizeof(double) + (size_t)2 * N * sizeof(double) +
                           (size_t)3 * N * sizeof(float));
 }
 
@@ -308,16 +321,18 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     const long m0 = (long)blockIdx.x * WPB;
     const long m = m0 + warp;
     double *const SA = SAall + warp * PKS;
-    double *const SX = SAall + WPB * PKS + warp * N;
+    double *const SX = SAall + WPB * PKS + warp * N;       // x
+    double *const SB = SAall + WPB * (PKS + N) + warp * N; // b, the right-hand side being solved
     // the pivot column twice over (SC, 16-byte aligned: N is a multiple of 8)
     // and the vector of a matrix-vector product (SR)
-    float *const SC = reinterpret_cast<float *>(SAall + WPB * (PKS + N)) + warp * 3 * N;
+    float *const SC = reinterpret_cast<float *>(SAall + WPB * (PKS + 2 * N)) + warp * 3 * N;
     float *const SR = SC + 2 * N;
 
     // ---- stage the block's matrices: packed lower triangles, identity past n ----
-    // thread t copies matrix t % WPB, rows t / WPB + 32 s of each column:
-    // a warp's loads cover WPB neighbouring lanes of eight rows (whole
-    // 32-byte sectors), and its stores two wavefronts
+    // Thread t copies matrix t % WPB, rows t / WPB + 32 s of each column, with
+    // asynchronous 8-byte copies (all of a thread's copies in flight at once):
+    // a warp's copies cover WPB neighbouring lanes of eight rows (whole 32-byte
+    // sectors), and its shared-memory writes two wavefronts.
     {
         LV<double> A0 = lv_make<double>(ap, row, ldap, V);
         if (up) A0 = A0.t();
@@ -336,12 +351,14 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
             for (int s = 0; s < (N + 31) / 32; ++s) {
                 const int i = j + rr + 32 * s;
                 if (i < N) {
-                    double a = (i == j) ? 1.0 : 0.0;
-                    if (jn && i < n) a = colp[(long)i * A0.si];
-                    Sj[i] = a;
+                    if (jn && i < n)
+                        cp_async8(Sj + i, colp + (long)i * A0.si);
+                    else
+                        Sj[i] = (i == j) ? 1.0 : 0.0;
                 }
             }
         }
+        cp_async_wait_all();
     }
     __syncthreads();
     if (m >= nlanes) return;
@@ -569,14 +586,15 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     float worst = 0.f;
     for (; col < nrhs && status == 0; ++col) {
         // all FP64 <-> FP32 conversions here are integer operations; w holds
-        // D b and then D r (the scaling folded into the exponent). x lives in
-        // SX and b is re-read from B: registers are kept for the FP32 rows.
+        // D b and then D r (the scaling folded into the exponent). x and b
+        // live in shared memory: registers are kept for the FP32 rows.
         float w[NR];
         float bn = 0.f;
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             const int i = lane + 32 * r;
             const double b = (i < n) ? B(i, col) : 0.0;
+            if (i < N) SB[i] = b;
             bn = fmaxf(bn, fabsf(d2f_rz(b)));
             w[r] = d2f_rz(b, -h[r]);
         }
@@ -597,7 +615,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
             double acc[NR];
 #pragma unroll
             for (int r = 0; r < NR; ++r)
-                acc[r] = (lane + 32 * r < n) ? B(lane + 32 * r, col) : 0.0;
+                acc[r] = (lane + 32 * r < N) ? SB[lane + 32 * r] : 0.0;
             residual<N>(lane, SA, SX, acc, acc);
             float rn = 0.f;
             bool nan = false; // fmaxf drops a NaN: a NaN residual must stop the refinement
