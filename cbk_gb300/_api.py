@@ -76,6 +76,62 @@ def dposv_refined_compact(layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_
 __all__ += ["dposv_refined_compact", "dposv_refined_lwork"]
 
 
+def dposv_refined_host_lwork(layout: str, n: int, nrhs: int, ldap: int, ldbp: int, V: int,
+                             nm: int) -> int:
+    """Device workspace bytes of dposv_refined_compact_host (-1: illegal argument)."""
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_dposv_refined_compact_host_lwork
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char] + [ctypes.c_int] * 6
+    return int(f(layout.encode(), n, nrhs, ldap, ldbp, V, nm))
+
+
+def _host_ptr(a):
+    """Address of a host array: a numpy array, a CPU torch tensor, an int or None."""
+    if a is None or isinstance(a, int):
+        return a
+    if hasattr(a, "ctypes"):
+        return a.ctypes.data
+    if getattr(a, "is_cuda", False):
+        raise ValueError("dposv_refined_compact_host takes host arrays")
+    return a.data_ptr()
+
+
+def dposv_refined_compact_host(layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter=10,
+                               iters=None, berr=None, dwork=None, lwork=None, stream=None):
+    """The mixed-precision dposv on batches in host memory (numpy arrays or
+    CPU tensors; pinned memory lets the copies overlap the solves). dwork: a
+    CUDA tensor of at least dposv_refined_host_lwork(...) bytes, allocated
+    here when None. Returns info once every copy is done."""
+    import ctypes
+
+    from ._abi import _stream, lib
+    need = (dposv_refined_host_lwork(layout, n, nrhs, ldap, ldbp, V, nm)
+            if (n > 0 and nm > 0 and V > 0) else 0)
+    if dwork is None and need > 0:
+        import torch
+        dwork = torch.empty(need, dtype=torch.uint8, device="cuda")
+    f = lib().cbk_cuda_dposv_refined_compact_host
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_longlong, ctypes.c_void_p]
+    dptr = dwork if (dwork is None or isinstance(dwork, int)) else dwork.data_ptr()
+    wbytes = lwork if lwork is not None else (
+        dwork.numel() * dwork.element_size() if dwork is not None and not isinstance(dwork, int)
+        else 0)
+    st = _stream(stream) if (stream is not None or (dwork is not None and
+                                                     not isinstance(dwork, int))) else None
+    return f(layout.encode(), uplo.encode(), n, nrhs, _host_ptr(ap), ldap, _host_ptr(bp), ldbp, V,
+             nm, max_iter, _host_ptr(iters), _host_ptr(berr), dptr, wbytes, st)
+
+
+__all__ += ["dposv_refined_compact_host", "dposv_refined_host_lwork"]
+
+
 # ---------------------------------------------------------------------------
 # uneven orders: bucketed launches and their CUDA graphs
 # ---------------------------------------------------------------------------

@@ -485,6 +485,31 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                         work, lwork, S(st));
 }
 
+long long cbk_cuda_dposv_refined_compact_host_lwork(char layout, int n, int nrhs, int ldap,
+                                                    int ldbp, int V, int nm)
+{
+    const bool col = opt(layout, 'C'), row = opt(layout, 'R');
+    if ((!col && !row) || n < 0 || nrhs < 0 || ldap < max1(n) ||
+        ldbp < max1(row ? nrhs : n) || !vlen_ok(V) || nm < 0)
+        return -1;
+    return (long long)posv_refined_host_lwork(row, n, nrhs, ldap, ldbp, V, nm);
+}
+
+int cbk_cuda_dposv_refined_compact_host(char layout, char uplo, int n, int nrhs, double *ap,
+                                        int ldap, double *bp, int ldbp, int V, int nm,
+                                        int max_iter, int *iters, double *berr, void *dwork,
+                                        long long lwork, cbk_stream_t stream)
+{
+    bool row, up;
+    if (int e = sym_solve_args(layout, uplo, n, nrhs, ldap, ldbp, V, nm, row, up)) return e;
+    if (max_iter < 0) return -11;
+    if (n == 0 || nm == 0 || nrhs == 0) return 0;
+    const size_t need = posv_refined_host_lwork(row, n, nrhs, ldap, ldbp, V, nm);
+    if (dwork == nullptr || lwork < (long long)need) return -15;
+    return cuda_status(posv_refined_host(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter,
+                                         iters, berr, dwork, S(stream)));
+}
+
 // The refined solve for callers that cannot allocate: scratch from the
 // library's fixed array; a batch whose scratch would not fit is rejected as an
 // illegal nm (-10).

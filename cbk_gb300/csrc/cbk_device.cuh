@@ -70,6 +70,13 @@ __device__ __forceinline__ bool lane_of(long ngroups, int V, Lane &ln)
 
 template <typename T> __device__ __forceinline__ T rcp(T x) { return T(1) / x; }
 
+// max(a, b) that keeps a NaN (fmaxf drops it): a NaN residual norm must stop
+// a refinement rather than pass its convergence test
+__device__ __forceinline__ float fmax_nan(float a, float b)
+{
+    return (a > b || a != a) ? a : b;
+}
+
 // ---------------------------------------------------------------------
 // Cholesky / LDL^T of the lower triangle of a lane view
 // ---------------------------------------------------------------------

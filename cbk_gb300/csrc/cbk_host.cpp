@@ -1,0 +1,158 @@
+// cbk_host.cpp -- the refined SPD solve on host-memory batches: the copies
+// in and out pipelined with the solves.
+//
+// The reference's calling convention keeps every array in host memory
+// (include/cbk.h:218-234, its MKL-style adapter src/cbk_compat.cpp copies
+// nothing because its kernels run on the CPU). Here a host batch is cut into
+// chunks of whole groups that flow through NBUF device slots, each slot on its
+// own stream: while one chunk is solved, the next one is copied in and the
+// previous one out, so the time is close to that of the copies alone. A
+// chunk's groups are contiguous in the compact layout, so each of its arrays
+// moves as one contiguous copy: on a GB300 host link that runs at the link's
+// full rate, while 2-D copies of only the referenced triangle (half of A's
+// bytes) measured three times slower. B (X) is copied back; A is copied back
+// only for a chunk in which some lane fell back to the FP64 path (those lanes
+// then hold the FP64 factor, the others the unchanged input), so the results
+// in host memory are exactly the device entry point's.
+#include "cbk_launch.h"
+
+#include <algorithm>
+#include <cuda_runtime.h>
+
+namespace cbkcuda {
+
+namespace {
+
+constexpr int NBUF = 3;
+constexpr long CHUNKS = 16;         // chunks per batch, unless that makes them small
+constexpr long MIN_CHUNK_GROUPS = 256;
+
+inline size_t align256(size_t b)
+{
+    return (b + 255) & ~(size_t)255;
+}
+
+struct Plan {
+    long ngroups, chunk;   // groups in the batch and per chunk
+    size_t ga, gb;         // bytes of one group of A and of B
+    size_t a, b, it, be, cnt, ws, slot; // bytes of each part of one slot
+};
+
+Plan plan(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm)
+{
+    Plan p{};
+    p.ngroups = ((long)nm + V - 1) / V;
+    p.chunk = std::min(p.ngroups, std::max(MIN_CHUNK_GROUPS, (p.ngroups + CHUNKS - 1) / CHUNKS));
+    p.ga = (size_t)ldap * n * V * sizeof(double);
+    p.gb = (size_t)ldbp * (row ? n : nrhs) * V * sizeof(double);
+    const size_t lanes = (size_t)p.chunk * V;
+    p.a = align256(p.chunk * p.ga);
+    p.b = align256(p.chunk * p.gb);
+    p.it = align256(lanes * sizeof(int));
+    p.be = align256(lanes * sizeof(double));
+    p.cnt = 256;
+    p.ws = align256(posv_refined_lwork(n, nrhs, V, (int)lanes));
+    p.slot = p.a + p.b + p.it + p.be + p.cnt + p.ws;
+    return p;
+}
+
+} // namespace
+
+size_t posv_refined_host_lwork(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm)
+{
+    if (n <= 0 || nrhs <= 0 || nm <= 0) return 0;
+    return (size_t)NBUF * plan(row, n, nrhs, ldap, ldbp, V, nm).slot;
+}
+
+cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
+                              int ldbp, int V, int nm, int max_iter, int *iters, double *berr,
+                              void *dwork, cudaStream_t caller)
+{
+    const Plan p = plan(row, n, nrhs, ldap, ldbp, V, nm);
+    char *const ha = reinterpret_cast<char *>(ap);
+    char *const hb = reinterpret_cast<char *>(bp);
+
+    struct Slot {
+        cudaStream_t s = nullptr;
+        double *a, *b, *be;
+        int *it, *cnt;
+        void *ws;
+        long g0 = -1, groups = 0; // the chunk in the slot (-1: none)
+    } slot[NBUF];
+    char *base = static_cast<char *>(dwork);
+    for (int k = 0; k < NBUF; ++k) {
+        char *q = base + (size_t)k * p.slot;
+        slot[k].a = reinterpret_cast<double *>(q);
+        slot[k].b = reinterpret_cast<double *>(q + p.a);
+        slot[k].it = reinterpret_cast<int *>(q + p.a + p.b);
+        slot[k].be = reinterpret_cast<double *>(q + p.a + p.b + p.it);
+        slot[k].cnt = reinterpret_cast<int *>(q + p.a + p.b + p.it + p.be);
+        slot[k].ws = p.ws ? q + p.a + p.b + p.it + p.be + p.cnt : nullptr;
+    }
+
+    cudaError_t err = cudaSuccess;
+    cudaEvent_t start = nullptr;
+    auto keep = [&](cudaError_t e) {
+        if (err == cudaSuccess && e != cudaSuccess) err = e;
+        return err == cudaSuccess;
+    };
+    // the slots' streams start after the caller's prior work on its stream
+    keep(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    if (err == cudaSuccess) keep(cudaEventRecord(start, caller));
+    for (int k = 0; k < NBUF && err == cudaSuccess; ++k)
+        if (keep(cudaStreamCreateWithFlags(&slot[k].s, cudaStreamNonBlocking)))
+            keep(cudaStreamWaitEvent(slot[k].s, start, 0));
+
+    // a chunk is finished once its stream is idle; if one of its lanes fell
+    // back, its A goes back to the host too
+    auto finish = [&](Slot &sl) {
+        if (sl.g0 < 0) return;
+        if (!keep(cudaStreamSynchronize(sl.s))) return;
+        int fell = 0;
+        if (keep(cudaMemcpyAsync(&fell, sl.cnt, sizeof(int), cudaMemcpyDeviceToHost, sl.s)) &&
+            keep(cudaStreamSynchronize(sl.s)) && fell > 0) {
+            keep(cudaMemcpyAsync(ha + (size_t)sl.g0 * p.ga, sl.a, (size_t)sl.groups * p.ga,
+                                 cudaMemcpyDeviceToHost, sl.s));
+            keep(cudaStreamSynchronize(sl.s));
+        }
+        sl.g0 = -1;
+    };
+
+    for (long g0 = 0, c = 0; g0 < p.ngroups && err == cudaSuccess; g0 += p.chunk, ++c) {
+        Slot &sl = slot[c % NBUF];
+        finish(sl);
+        if (err != cudaSuccess) break;
+        const long groups = std::min(p.chunk, p.ngroups - g0);
+        const long lane0 = g0 * V;
+        const int nmc = (int)std::min((long)nm - lane0, groups * V);
+        keep(cudaMemsetAsync(sl.cnt, 0, sizeof(int), sl.s));
+        keep(cudaMemcpyAsync(sl.a, ha + (size_t)g0 * p.ga, (size_t)groups * p.ga,
+                             cudaMemcpyHostToDevice, sl.s));
+        keep(cudaMemcpyAsync(sl.b, hb + (size_t)g0 * p.gb, (size_t)groups * p.gb,
+                             cudaMemcpyHostToDevice, sl.s));
+        keep(launch_posv_refined(row, up, n, nrhs, sl.a, ldap, sl.b, ldbp, V, nmc, max_iter, sl.it,
+                                 berr ? sl.be : nullptr, sl.ws, sl.s));
+        keep(launch_count_negative(sl.it, nmc, sl.cnt, sl.s));
+        keep(cudaMemcpyAsync(hb + (size_t)g0 * p.gb, sl.b, (size_t)groups * p.gb,
+                             cudaMemcpyDeviceToHost, sl.s));
+        if (iters)
+            keep(cudaMemcpyAsync(iters + lane0, sl.it, (size_t)nmc * sizeof(int),
+                                 cudaMemcpyDeviceToHost, sl.s));
+        if (berr)
+            keep(cudaMemcpyAsync(berr + lane0, sl.be, (size_t)nmc * sizeof(double),
+                                 cudaMemcpyDeviceToHost, sl.s));
+        sl.g0 = g0;
+        sl.groups = groups;
+    }
+    for (int k = 0; k < NBUF; ++k)
+        if (err == cudaSuccess) finish(slot[k]);
+    for (int k = 0; k < NBUF; ++k)
+        if (slot[k].s) {
+            cudaStreamSynchronize(slot[k].s);
+            cudaStreamDestroy(slot[k].s);
+        }
+    if (start) cudaEventDestroy(start);
+    return err;
+}
+
+} // namespace cbkcuda

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(128)
                 for (int j = 0; j < N; ++j)
                     acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
                 z[i] = (float)acc;
-                rnorm = fmaxf(rnorm, fabsf(z[i]));
+                rnorm = fmax_nan(rnorm, fabsf(z[i]));
                 xnorm = fmaxf(xnorm, fabsf(x32[i]));
             }
             if ((double)rnorm <= cte * (double)xnorm) {
@@ -275,7 +275,7 @@ __device__ __forceinline__ void resid_rows(int n, int i0, int col, LV<double> A,
     for (int r = 0; r < NR; ++r) {
         const float z = (float)acc[r];
         Z[(long)(i0 + r) * V] = z;
-        rnorm = fmaxf(rnorm, fabsf(z));
+        rnorm = fmax_nan(rnorm, fabsf(z));
     }
 }
 
@@ -429,6 +429,25 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
     w.z = reinterpret_cast<float *>(base);
     k_posv_refined_ws<<<bl, th, 0, s>>>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, ng, sa, sb, w,
                                         out);
+    return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void k_count_negative(const int *iters, int n, int *count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool neg = i < n && iters[i] < 0;
+    const unsigned b = __ballot_sync(0xffffffffu, neg);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, __popc(b));
+}
+
+} // namespace
+
+cudaError_t launch_count_negative(const int *iters, int n, int *count, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_count_negative<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(iters, n, count);
     return cudaGetLastError();
 }
 

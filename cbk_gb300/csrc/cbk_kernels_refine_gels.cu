@@ -138,14 +138,14 @@ __global__ void __launch_bounds__(128, 4)
                 }
                 const float fi = (float)acc;
                 W[(long)i * V] = fi;
-                fn = fmaxf(fn, fabsf(fi));
+                fn = fmax_nan(fn, fabsf(fi));
                 rn = fmaxf(rn, fabsf((float)ri));
             }
             float h[GELS_NMAX];
             float gn = 0.f;
             for (int j = 0; j < n; ++j) {
                 h[j] = (float)g[j];
-                gn = fmaxf(gn, fabsf(h[j]));
+                gn = fmax_nan(gn, fabsf(h[j]));
                 xn = fmaxf(xn, fabsf((float)x[j]));
             }
             const double scale = (double)anorm * xn + bn;

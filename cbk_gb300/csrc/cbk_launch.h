@@ -96,6 +96,15 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
                                      double *bp, int ldbp, int V, int nm, int max_iter,
                                      int *iters, double *berr, cudaStream_t s);
 
+// the refined solve on host-memory batches, copies pipelined with the solves
+// (cbk_host.cpp); dwork: device workspace of posv_refined_host_lwork bytes
+size_t posv_refined_host_lwork(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm);
+cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
+                              int ldbp, int V, int nm, int max_iter, int *iters, double *berr,
+                              void *dwork, cudaStream_t caller);
+// *count += the number of negative entries of iters[0 .. n)
+cudaError_t launch_count_negative(const int *iters, int n, int *count, cudaStream_t s);
+
 // the same with the library's own scratch array (no allocation, no workspace)
 cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                         double *bp, int ldbp, int V, int nm, int max_iter,

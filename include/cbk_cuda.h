@@ -250,6 +250,30 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                                          int max_iter, int *iters, double *berr, void *work,
                                          long long lwork, cbk_stream_t stream);
 
+/* The same solve on batches in HOST memory (ap, bp, iters, berr are host
+ * pointers; pinned memory lets the copies overlap the solves). No reference
+ * entry point: the reference's own calling convention -- every array on the
+ * host, as in ?posv_compact (include/cbk.h:218-234) -- over the device solve
+ * above. The batch is cut into chunks of whole groups that pass through
+ * three device slots on three streams, so that copying one chunk in, solving
+ * another and copying a third out overlap; each chunk's A and B move as one
+ * contiguous copy each. B (X) is copied back; A is copied back only for a
+ * chunk in which some lane fell back (ap then holds those lanes' FP64
+ * factor), so ap, bp, iters and berr end exactly as the device entry point
+ * leaves them. dwork is a device workspace of at least
+ * cbk_cuda_dposv_refined_compact_host_lwork(layout, n, nrhs, ldap, ldbp, V,
+ * nm) bytes (0 when n, nrhs or nm is 0; -1 for an illegal argument). The call
+ * returns when every copy is done; its work is ordered after the caller's
+ * prior work on stream. Returns 0, the codes of
+ * cbk_cuda_dposv_refined_compact_async (-15 for dwork/lwork), or
+ * CBK_CUDA_ERROR_BASE + a CUDA error. */
+long long cbk_cuda_dposv_refined_compact_host_lwork(char layout, int n, int nrhs, int ldap,
+                                                    int ldbp, int V, int nm);
+int cbk_cuda_dposv_refined_compact_host(char layout, char uplo, int n, int nrhs, double *ap,
+                                        int ldap, double *bp, int ldbp, int V, int nm,
+                                        int max_iter, int *iters, double *berr, void *dwork,
+                                        long long lwork, cbk_stream_t stream);
+
 /* Mixed-precision least squares min ||b - A x||, A m x n with m >= n: FP32
  * QR, FP64 refinement of the augmented system [I A; A^T 0][r; x] = [b; 0]
  * (Bjorck) per right-hand side, FP64 fallback per matrix. No reference entry

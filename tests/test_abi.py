@@ -125,3 +125,28 @@ def test_bucketed_argument_checks():
     assert f(b"C", b"L", 2, 2, a(ok), fake_work, 255, None) == -7
     assert f(b"C", b"L", 2, 2, a(empty), fake_work, 256, None) == 0
     assert f(b"C", b"L", 2, 0, None, fake_work, 256, None) == 0
+
+
+def test_refined_host_entry_validates_before_any_device_work():
+    """cbk_cuda_dposv_refined_compact_host checks its arguments in order and
+    returns before touching a pointer or the device (here: no GPU at all)."""
+    import cbk_gb300
+    f = cbk_gb300.dposv_refined_compact_host
+    assert f("X", "L", 8, 1, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == -1
+    assert f("C", "Q", 8, 1, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == -2
+    assert f("C", "L", -1, 1, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == -3
+    assert f("C", "L", 8, -1, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == -4
+    assert f("C", "L", 8, 1, None, 7, None, 8, 32, 64, dwork=0, lwork=0) == -6
+    assert f("C", "L", 8, 1, None, 8, None, 7, 32, 64, dwork=0, lwork=0) == -8
+    assert f("C", "L", 8, 1, None, 8, None, 8, 33, 64, dwork=0, lwork=0) == -9
+    assert f("C", "L", 8, 1, None, 8, None, 8, 32, -1, dwork=0, lwork=0) == -10
+    assert f("C", "L", 8, 1, None, 8, None, 8, 32, 64, max_iter=-1, dwork=0, lwork=0) == -11
+    assert f("C", "L", 8, 1, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == -15
+    assert f("C", "L", 8, 0, None, 8, None, 8, 32, 64, dwork=0, lwork=0) == 0
+    lw = cbk_gb300.dposv_refined_host_lwork
+    assert lw("C", 8, 1, 8, 8, 32, 0) == 0 and lw("C", 8, 1, 8, 8, 33, 64) == -1
+    assert lw("X", 8, 1, 8, 8, 32, 64) == -1 and lw("C", 8, 1, 7, 8, 32, 64) == -1
+    # three slots, each with a chunk of at least 256 groups (or the batch)
+    assert lw("C", 48, 1, 48, 48, 32, 64) >= 3 * 32 * 48 * 48 * 8
+    assert lw("C", 48, 1, 50, 48, 32, 64) > lw("C", 48, 1, 48, 48, 32, 64)
+    assert lw("C", 48, 1, 48, 48, 32, 10 ** 6) < lw("C", 48, 1, 48, 48, 32, 2 * 10 ** 6)
