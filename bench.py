@@ -83,6 +83,26 @@ def dist_setup():
     return ws, rank, local
 
 
+def slowest_rank(times_ms, device=None):
+    """Each timing's maximum over ranks (the slowest rank decides): an
+    all-reduce MAX when torch.distributed runs more than one rank, the values
+    themselves otherwise. device: where the reduction tensor lives (a CUDA
+    device under NCCL, the CPU under gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(t) for t in times_ms]
+    tt = torch.tensor([float(t) for t in times_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return [float(x) for x in tt]
+
+
+def job_throughput(units_per_rank, t_ms, ws):
+    """Whole-job throughput of weak-scaled replicas: every rank's units over
+    the slowest rank's time."""
+    return ws * units_per_rank / (t_ms * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampler over the timed region (clocks, throttle reasons)."""
 
@@ -379,13 +399,9 @@ def run_gpu(args):
     solves = NM * len(SIZES)
     t_ref = sum(ref_tot) / len(ref_tot)
     t_pl = sum(pl_tot) / len(pl_tot)
-    # slowest rank decides
-    if ws > 1:
-        tt = torch.tensor([t_ref, t_pl], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ref, t_pl = float(tt[0]), float(tt[1])
-    value = ws * solves / (t_ref * 1e-3)
-    plain_value = ws * solves / (t_pl * 1e-3)
+    t_ref, t_pl = slowest_rank([t_ref, t_pl], dev)
+    value = job_throughput(solves, t_ref, ws)
+    plain_value = job_throughput(solves, t_pl, ws)
 
     per_n = {}
     for k, b in enumerate(batches):
@@ -517,13 +533,8 @@ def e2e(args, cbk, batches, barrier, ws):
     for _ in range(max(1, args.warmup // 2)):
         one()
     ts = [one() for _ in range(args.steps)]
-    t = sum(ts) / len(ts)
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t], dtype=torch.float64, device=batches[0]["ap"].device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt[0])
-    return {"value": ws * NM * len(SIZES) / (t * 1e-3), "unit": UNIT, "ms_per_step": t,
+    t = slowest_rank([sum(ts) / len(ts)], batches[0]["ap"].device)[0]
+    return {"value": job_throughput(NM * len(SIZES), t, ws), "unit": UNIT, "ms_per_step": t,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "path": "cbk_cuda_dposv_refined_compact_host per n: pinned host A and b in, x "
                     "out, contiguous copies per chunk pipelined with the solves in 3 device "

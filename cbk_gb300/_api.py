@@ -275,3 +275,93 @@ def dgels_refined_compact(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V
 
 
 __all__ += ["dgels_refined_compact", "dgels_refined_lwork"]
+
+
+# ---------------------------------------------------------------------------
+# autotuning
+# ---------------------------------------------------------------------------
+
+def _tune_struct():
+    import ctypes
+
+    class TuneResult(ctypes.Structure):
+        _fields_ = [("threads", ctypes.c_int), ("variant", ctypes.c_int), ("vlen", ctypes.c_int),
+                    ("ms", ctypes.c_double)]
+    return TuneResult
+
+
+_TUNE = []
+
+
+def _tr():
+    if not _TUNE:
+        _TUNE.append(_tune_struct())
+    return _TUNE[0]
+
+
+def autotune(routine: str, prec: str, m: int, n: int, nrhs: int, nm: int):
+    """Time the routine's launch shapes and widths on a synthetic batch and
+    keep the fastest in the library's table. Returns (info, dict)."""
+    import ctypes
+
+    from ._abi import lib
+    TR = _tr()
+    f = lib().cbk_cuda_autotune
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_char] + [ctypes.c_int] * 4 + [ctypes.POINTER(TR)]
+    r = TR()
+    info = f(routine.encode(), prec.encode(), m, n, nrhs, nm, ctypes.byref(r))
+    return info, {"threads": r.threads, "variant": r.variant, "vlen": r.vlen, "ms": r.ms}
+
+
+def tune_set(routine: str, prec: str, n: int, threads: int = 0, variant: int = 0,
+             vlen: int = 0) -> int:
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_tune_set
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_char] + [ctypes.c_int] * 4
+    return f(routine.encode(), prec.encode(), n, threads, variant, vlen)
+
+
+def tune_get(routine: str, prec: str, n: int):
+    """(info, {"threads", "variant", "vlen"}) of one table entry."""
+    import ctypes
+
+    from ._abi import lib
+    TR = _tr()
+    f = lib().cbk_cuda_tune_get
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_char, ctypes.c_int, ctypes.POINTER(TR)]
+    r = TR()
+    info = f(routine.encode(), prec.encode(), n, ctypes.byref(r))
+    return info, {"threads": r.threads, "variant": r.variant, "vlen": r.vlen}
+
+
+def tune_reset() -> None:
+    from ._abi import lib
+    lib().cbk_cuda_tune_reset()
+
+
+def tune_save(path: str) -> int:
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_tune_save
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p]
+    return f(path.encode())
+
+
+def tune_load(path: str) -> int:
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_tune_load
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p]
+    return f(path.encode())
+
+
+__all__ += ["autotune", "tune_set", "tune_get", "tune_reset", "tune_save", "tune_load"]

@@ -1,0 +1,266 @@
+// cbk_autotune.cu -- the autotuner: measured launch shapes and interleave
+// widths per (routine, precision, order).
+//
+// No counterpart in the reference (one code path per V, chosen by the
+// caller). cbk_cuda_autotune times a routine on a synthetic batch of nm
+// matrices generated on the device -- uniform entries in [-1, 1), with the
+// diagonal raised by n + 1 where the routine needs a positive-definite or
+// well-conditioned triangular matrix, and the factors computed first where
+// the routine consumes them (potrs, sytrsnp: the factor; ormqr, orgqr: the
+// QR) -- for every candidate shape: threads per block 64 / 128 / 256 for the
+// lane-per-matrix kernels (32 / 64 / 128 for the lane-per-matrix refined
+// solves, which are compiled for at most 128), the two register caps of the warp-per-matrix
+// refined solve (orders 17 .. 64), each at interleave widths 32, 64 and 128.
+// Each candidate is timed with CUDA events, best of three runs, inputs
+// restored from a pristine copy before each run. The winner goes into the
+// tuning table that every later launch reads (threads / variant for the
+// routine's order, and the width as advice for the caller's layout).
+// Launch shapes never change results, so tuning is safe at any time.
+#include "../../include/cbk_cuda.h"
+#include "cbk_launch.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cuda_runtime.h>
+
+namespace cbkcuda {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
+{
+    // splitmix64's finaliser (Steele, Lea, Flood 2014)
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// a[i] = uniform [-1, 1) from (seed, i)
+template <typename T> __global__ void k_fill_uniform(T *a, long count, unsigned long long seed)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < count;
+         i += (long)gridDim.x * blockDim.x)
+        a[i] = (T)((double)(mix64(seed ^ (unsigned long long)i) >> 11) * 0x1p-52 - 1.0);
+}
+
+// A(i, i) += shift for every lane of a column-major compact batch (ld = n)
+template <typename T> __global__ void k_shift_diag(T *a, int n, int V, long lanes, T shift)
+{
+    const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (l >= lanes) return;
+    const long g = l / V;
+    const int v = (int)(l - g * V);
+    T *p = a + g * (long)n * n * V + v;
+    for (int i = 0; i < n; ++i)
+        p[((long)i * n + i) * V] += shift;
+}
+
+template <typename T> struct Batch {
+    int m, n, nrhs, V, nm;
+    long lanes;
+    T *a = nullptr, *a0 = nullptr, *b = nullptr, *b0 = nullptr, *tau = nullptr;
+    void *ws = nullptr;
+    size_t sa = 0, sb = 0, ws_bytes = 0;
+};
+
+template <typename T> void release(Batch<T> &B)
+{
+    cudaFree(B.a);
+    cudaFree(B.a0);
+    cudaFree(B.b);
+    cudaFree(B.b0);
+    cudaFree(B.tau);
+    cudaFree(B.ws);
+    B = Batch<T>{};
+}
+
+enum Kind { FACTOR, SOLVE, FUSED, TRSM, GEQRF, ORMQR, ORGQR, GELS, REFINED };
+
+struct Spec {
+    int routine;
+    Kind kind;
+    bool ldlt;
+    bool spd;  // diagonal raised
+    int key;   // the order the launcher keys the table on
+};
+
+template <typename T>
+cudaError_t run(const Spec &sp, Batch<T> &B, cudaStream_t s)
+{
+    const int m = B.m, n = B.n, nrhs = B.nrhs, V = B.V, nm = B.nm;
+    switch (sp.kind) {
+    case FACTOR: return launch_factor<T>(sp.ldlt, false, false, n, B.a, n, V, nm, s);
+    case SOLVE:
+        return launch_sym_solve<T>(sp.ldlt, false, false, false, n, nrhs, B.a, n, B.b, n, V, nm, s);
+    case FUSED:
+        return launch_sym_solve<T>(sp.ldlt, true, false, false, n, nrhs, B.a, n, B.b, n, V, nm, s);
+    case TRSM:
+        return launch_trsm<T>(true, false, false, false, false, n, nrhs, T(1), B.a, n, B.b, n, V,
+                              nm, s);
+    case GEQRF: return launch_geqrf<T>(false, m, n, B.a, m, B.tau, V, nm, s);
+    case ORMQR:
+        return launch_ormqr<T>(true, false, true, m, nrhs, n, B.a, m, B.tau, B.b, m, V, nm, s);
+    case ORGQR: return launch_orgqr<T>(false, m, n, n, B.a, m, B.tau, V, nm, s);
+    case GELS: return launch_gels<T>(false, false, m, n, nrhs, B.a, m, B.b, m, B.tau, V, nm, s);
+    case REFINED:
+        if constexpr (sizeof(T) == 8)
+            return launch_posv_refined(false, false, n, nrhs, B.a, n, B.b, n, V, nm, 10, nullptr,
+                                       nullptr, B.ws, s);
+        return cudaErrorInvalidValue;
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t make_batch(const Spec &sp, int m, int n, int nrhs, int V, int nm, Batch<T> &B,
+                       cudaStream_t s)
+{
+    B.m = m;
+    B.n = n;
+    B.nrhs = nrhs;
+    B.V = V;
+    B.nm = nm;
+    B.lanes = ((long)nm + V - 1) / V * V;
+    const int rows = (sp.kind == GEQRF || sp.kind == ORMQR || sp.kind == ORGQR ||
+                      sp.kind == GELS) ? m : n;
+    B.sa = (size_t)B.lanes * rows * n;
+    B.sb = (size_t)B.lanes * std::max(rows, 1) * std::max(nrhs, 1);
+    cudaError_t e;
+    if ((e = cudaMalloc(&B.a, B.sa * sizeof(T))) || (e = cudaMalloc(&B.a0, B.sa * sizeof(T))) ||
+        (e = cudaMalloc(&B.b, B.sb * sizeof(T))) || (e = cudaMalloc(&B.b0, B.sb * sizeof(T))) ||
+        (e = cudaMalloc(&B.tau, (size_t)B.lanes * std::max(std::min(m, n), 1) * sizeof(T))))
+        return e;
+    if (sp.kind == REFINED) {
+        B.ws_bytes = posv_refined_lwork(n, nrhs, V, nm);
+        if (B.ws_bytes && (e = cudaMalloc(&B.ws, B.ws_bytes))) return e;
+    }
+    const unsigned grid = 1024;
+    k_fill_uniform<T><<<grid, 256, 0, s>>>(B.a0, (long)B.sa, 0x5EEDull);
+    k_fill_uniform<T><<<grid, 256, 0, s>>>(B.b0, (long)B.sb, 0xB0Bull);
+    if (sp.spd)
+        k_shift_diag<T><<<(unsigned)((B.lanes + 255) / 256), 256, 0, s>>>(B.a0, n, V, B.lanes,
+                                                                          T(n + 1));
+    if ((e = cudaGetLastError())) return e;
+    // routines that consume a factorization get it once, untimed
+    if (sp.kind == SOLVE) e = launch_factor<T>(sp.ldlt, false, false, n, B.a0, n, V, nm, s);
+    if (sp.kind == ORMQR || sp.kind == ORGQR) e = launch_geqrf<T>(false, m, n, B.a0, m, B.tau, V, nm, s);
+    return e;
+}
+
+template <typename T>
+cudaError_t time_one(const Spec &sp, Batch<T> &B, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
+                     float &best)
+{
+    best = FLT_MAX;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(B.a, B.a0, B.sa * sizeof(T), cudaMemcpyDeviceToDevice, s)) ||
+            (e = cudaMemcpyAsync(B.b, B.b0, B.sb * sizeof(T), cudaMemcpyDeviceToDevice, s)) ||
+            (e = cudaEventRecord(e0, s)) || (e = run<T>(sp, B, s)) || (e = cudaEventRecord(e1, s)) ||
+            (e = cudaEventSynchronize(e1)))
+            return e;
+        float ms = 0.f;
+        if ((e = cudaEventElapsedTime(&ms, e0, e1))) return e;
+        if (rep > 0) best = std::min(best, ms); // the first run warms up
+    }
+    return cudaSuccess;
+}
+
+template <typename T>
+int autotune(const Spec &sp, int m, int n, int nrhs, int nm, const cbk_cuda_tune_result &old,
+             cbk_cuda_tune_result *out)
+{
+    constexpr int ds = sizeof(T);
+    const bool warp = sp.kind == REFINED && posv_refined_warp_ok(n);
+    const int widths[] = {32, 64, 128};
+    // the lane-per-matrix refined kernels are compiled for at most 128 threads
+    const int lane_threads[] = {64, 128, 256}, refined_threads[] = {32, 64, 128};
+    const int *threads = sp.kind == REFINED ? refined_threads : lane_threads;
+    const int nshape = warp ? MAX_VARIANTS : 3;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (!err) err = cudaEventCreate(&e0);
+    if (!err) err = cudaEventCreate(&e1);
+    float best = FLT_MAX;
+    int best_shape = 0, best_V = 32;
+    for (int V : widths) {
+        if (err) break;
+        Batch<T> B;
+        err = make_batch<T>(sp, m, n, nrhs, V, nm, B, s);
+        for (int k = 0; k < nshape && !err; ++k) {
+            if (warp) set_variant(sp.routine, sp.key, ds, k);
+            else set_threads(sp.routine, sp.key, ds, threads[k]);
+            float ms = 0.f;
+            err = time_one<T>(sp, B, s, e0, e1, ms);
+            if (!err && ms < best) {
+                best = ms;
+                best_shape = k;
+                best_V = V;
+            }
+        }
+        cudaStreamSynchronize(s);
+        release(B);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (err) { // the entry keeps what it held before the search
+        set_variant(sp.routine, sp.key, ds, old.variant);
+        set_threads(sp.routine, sp.key, ds, old.threads);
+        return CBK_CUDA_ERROR_BASE + (int)err;
+    }
+    if (warp) set_variant(sp.routine, sp.key, ds, best_shape);
+    else set_threads(sp.routine, sp.key, ds, threads[best_shape]);
+    set_vlen(sp.routine, sp.key, ds, best_V);
+    if (out) {
+        out->threads = warp ? 0 : threads[best_shape];
+        out->variant = warp ? best_shape : 0;
+        out->vlen = best_V;
+        out->ms = best;
+    }
+    return 0;
+}
+
+} // namespace
+
+} // namespace cbkcuda
+
+using namespace cbkcuda;
+
+extern "C" int cbk_cuda_autotune(const char *routine, char prec, int m, int n, int nrhs, int nm,
+                                 cbk_cuda_tune_result *out)
+{
+    const int r = routine_of(routine);
+    if (r < 0) return -1;
+    if (prec != 'd' && prec != 's') return -2;
+    const bool qr = r == R_GEQRF || r == R_ORMQR || r == R_ORGQR || r == R_GELS;
+    if (m < 0 || (qr && m < n)) return -3;
+    if (n < 1) return -4;
+    const bool rhs = r == R_POTRS || r == R_POSV || r == R_SYTRSNP || r == R_SYSVNP ||
+                     r == R_TRSM || r == R_ORMQR || r == R_GELS || r == R_POSV_REFINED;
+    if (nrhs < (rhs ? 1 : 0)) return -5;
+    if (nm < 1) return -6;
+    if (r == R_POSV_REFINED && prec != 'd') return -2;
+    Spec sp{r, FACTOR, false, false, n};
+    switch (r) {
+    case R_POTRF: sp = {r, FACTOR, false, true, n}; break;
+    case R_SYTRFNP: sp = {r, FACTOR, true, true, n}; break;
+    case R_POTRS: sp = {r, SOLVE, false, true, n}; break;
+    case R_SYTRSNP: sp = {r, SOLVE, true, true, n}; break;
+    case R_POSV: sp = {r, FUSED, false, true, n}; break;
+    case R_SYSVNP: sp = {r, FUSED, true, true, n}; break;
+    case R_TRSM: sp = {r, TRSM, false, true, n}; break;
+    case R_GEQRF: sp = {r, GEQRF, false, false, m}; break;
+    case R_ORMQR: sp = {r, ORMQR, false, false, m}; break;
+    case R_ORGQR: sp = {r, ORGQR, false, false, m}; break;
+    case R_GELS: sp = {r, GELS, false, false, m}; break;
+    case R_POSV_REFINED: sp = {r, REFINED, false, true, n}; break;
+    default: return -1;
+    }
+    cbk_cuda_tune_result old{};
+    cbk_cuda_tune_get(routine, prec, sp.key, &old);
+    return prec == 'd' ? autotune<double>(sp, m, n, nrhs, nm, old, out)
+                       : autotune<float>(sp, m, n, nrhs, nm, old, out);
+}

@@ -33,6 +33,8 @@
 #include "cbk_device.cuh"
 #include "cbk_launch.h"
 
+#include <algorithm>
+
 #include "../../include/cbk_cuda.h"
 
 #include <atomic>
@@ -398,7 +400,8 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
     const long ng = ((long)nm + V - 1) / V;
     const size_t sa = gstride(row, ldap, n, n, V), sb = gstride(row, ldbp, n, nrhs, V);
     const RefineOut out{iters, berr, nm, max_iter};
-    const int th = 128;
+    // the lane-per-matrix variants are compiled for at most 128 threads
+    const int th = std::min(threads_for(R_POSV_REFINED, n, sizeof(double)), 128);
     const unsigned bl = (unsigned)((ng * V + th - 1) / th);
     if (n <= REG_NMAX) {
         switch (n) {

@@ -20,6 +20,13 @@ void set_threads(int routine, int n, int dsize, int threads);
 constexpr int MAX_VARIANTS = 2;
 int variant_for(int routine, int n, int dsize);
 void set_variant(int routine, int n, int dsize, int variant);
+// the interleave width measured fastest (0: untuned)
+int vlen_for(int routine, int n, int dsize);
+void set_vlen(int routine, int n, int dsize, int V);
+// routine names of the tuning API ("posv", "posv_refined", ...) <-> Routine
+int routine_of(const char *name);
+const char *routine_name(int routine);
+int tune_slots();
 
 enum Routine {
     R_POTRF = 0, R_SYTRFNP, R_POTRS, R_POSV, R_SYTRSNP, R_SYSVNP, R_TRSM, R_GEQRF, R_ORMQR,

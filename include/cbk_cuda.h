@@ -388,6 +388,44 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
                                                  int V, int nm, int max_iter, int *iters,
                                                  double *berr, cbk_stream_t stream);
 
+/* Autotuning, no reference counterpart. The library keeps one process-wide
+ * table of launch shapes per (routine, precision, order): threads per block
+ * of the lane-per-matrix kernels, the kernel variant of the warp-per-matrix
+ * refined solve (orders 17 .. 64), and the interleave width measured fastest
+ * (advice for the caller's packing; a batch's width is the caller's). Entry
+ * 0 means the built-in choice. Launch shapes never change results.
+ * routine: "potrf", "sytrfnp", "potrs", "posv", "sytrsnp", "sysvnp", "trsm",
+ * "geqrf", "ormqr", "orgqr", "gels" or "posv_refined"; prec 'd' or 's' ('d'
+ * only for posv_refined); the order is n, except m for the QR routines.
+ *
+ * cbk_cuda_autotune times the routine on a synthetic batch of nm matrices
+ * (m x n for the QR routines, m >= n; n x n otherwise; nrhs right-hand
+ * sides) for every candidate shape at widths 32, 64 and 128, best of three
+ * CUDA-event timings each, and stores the winner. It allocates and
+ * synchronises the device (not for use inside a stream capture). Returns 0,
+ * -1 routine, -2 prec, -3 m, -4 n, -5 nrhs, -6 nm, or CBK_CUDA_ERROR_BASE + a
+ * CUDA error (the table entry then keeps the built-in choice).
+ * cbk_cuda_tune_set / _get write / read one entry (set: threads 0 or a
+ * power of two 32 .. 512, variant 0 or 1, vlen 0 or a multiple of 32 up to
+ * 1024; -j for the first illegal argument). cbk_cuda_tune_save writes every
+ * non-default entry as text ("routine prec n threads variant vlen" lines);
+ * cbk_cuda_tune_load reads such a file and returns the number of entries, -1
+ * if it cannot be read, or -(line) at the first malformed line. The
+ * environment variable CBK_CUDA_TUNE_FILE names a file loaded on first use. */
+typedef struct {
+    int threads; /* threads per block (0: built-in) */
+    int variant; /* kernel variant (0: built-in) */
+    int vlen;    /* fastest interleave width measured (0: untuned) */
+    double ms;   /* the chosen shape's time for the tuning batch (autotune only) */
+} cbk_cuda_tune_result;
+int cbk_cuda_autotune(const char *routine, char prec, int m, int n, int nrhs, int nm,
+                      cbk_cuda_tune_result *out);
+int cbk_cuda_tune_set(const char *routine, char prec, int n, int threads, int variant, int vlen);
+int cbk_cuda_tune_get(const char *routine, char prec, int n, cbk_cuda_tune_result *out);
+void cbk_cuda_tune_reset(void);
+int cbk_cuda_tune_save(const char *path);
+int cbk_cuda_tune_load(const char *path);
+
 /* Calibration, no reference counterpart: the measured fused multiply-add
  * rate of the current device in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1)
  * or FP32 (fp64 = 0), from a ~10 ms synthetic kernel -- the denominator of the

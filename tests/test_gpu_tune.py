@@ -1,0 +1,70 @@
+"""The autotuner on the GPU: it measures, keeps a valid winner in the table,
+and no launch shape it can pick changes a result (bit-identical outputs for
+every threads-per-block choice and both refined-kernel variants)."""
+import numpy as np
+import pytest
+
+import cases as C
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def tune():
+    import cbk_gb300
+    cbk_gb300.tune_reset()
+    yield cbk_gb300
+    cbk_gb300.tune_reset()
+
+
+@pytest.mark.parametrize("routine,prec,m,n,nrhs", [
+    ("posv", "d", 16, 16, 1), ("sysvnp", "s", 12, 12, 2), ("geqrf", "d", 16, 8, 0),
+    ("gels", "d", 16, 8, 4), ("orgqr", "s", 16, 8, 0), ("posv_refined", "d", 48, 48, 1),
+    ("posv_refined", "d", 8, 8, 1)])
+def test_autotune_picks_a_measured_shape(tune, routine, prec, m, n, nrhs, cuda):
+    info, r = tune.autotune(routine, prec, m, n, nrhs, 4096)
+    assert info == 0
+    assert r["vlen"] in (32, 64, 128) and r["ms"] > 0
+    warp = routine == "posv_refined" and 16 < n <= 64
+    if warp:
+        assert r["variant"] in (0, 1) and r["threads"] == 0
+    elif routine == "posv_refined":
+        assert r["threads"] in (32, 64, 128)
+    else:
+        assert r["threads"] in (64, 128, 256)
+    key = m if routine in ("geqrf", "ormqr", "orgqr", "gels") else n
+    assert tune.tune_get(routine, prec, key)[1] == {k: r[k] for k in ("threads", "variant", "vlen")}
+
+
+def _solve(tune, A, B, V, refined):
+    import torch
+    nm, n, _ = A.shape
+    ap = torch.from_numpy(O.pack(A, V)).cuda()
+    bp = torch.from_numpy(O.pack(B, V, pad_diag=0.0)).cuda()
+    if refined:
+        it = torch.empty(nm, dtype=torch.int32, device="cuda")
+        assert tune.dposv_refined_compact("C", "L", n, 1, ap, n, bp, n, V, nm, iters=it) == 0
+    else:
+        assert tune.dposv_compact("C", "L", n, 1, ap, n, bp, n, V, nm) == 0
+    torch.cuda.synchronize()
+    return ap.cpu().numpy(), bp.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [8, 24, 48])
+def test_launch_shape_never_changes_results(tune, n, cuda):
+    rng = np.random.default_rng(n)
+    A, _ = C.gen_spd_cond(rng, 3000, n)
+    B = rng.standard_normal((3000, n, 1))
+    outs = []
+    for t in (64, 128, 256):
+        assert tune.tune_set("posv", "d", n, threads=t) == 0
+        outs.append(_solve(tune, A, B, 32, refined=False))
+    for o in outs[1:]:
+        assert all(np.array_equal(x, y) for x, y in zip(outs[0], o))
+    outs = []
+    for shape in ((64, 0), (256, 0), (0, 0), (0, 1)):
+        assert tune.tune_set("posv_refined", "d", n, threads=shape[0], variant=shape[1]) == 0
+        outs.append(_solve(tune, A, B, 32, refined=True))
+    for o in outs[1:]:
+        assert all(np.array_equal(x, y) for x, y in zip(outs[0], o))
