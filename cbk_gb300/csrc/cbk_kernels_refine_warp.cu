@@ -258,52 +258,81 @@ __device__ __forceinline__ void apply_inverse(int lane, const float (&R0)[N],
     }
 }
 
+// A(i, j) of the packed triangle for a static column j: row i's own part
+// (j <= i) at lo[pk_col(N, j) - j] with lo = SA + i, or column i's part
+// (j > i) at hi[j] with hi = SA + pk_col(N, i) - i. Two predicated loads from
+// per-lane bases with constant offsets: no index arithmetic per element.
+template <int N>
+__device__ __forceinline__ double tri_at(const double *lo, const double *hi, int i, int j)
+{
+    double a;
+    if (j <= i)
+        a = lo[pk_col(N, j) - j];
+    else
+        a = hi[j];
+    return a;
+}
+
 // acc[r] := b[r] - (A x)(row lane + 32 r) from the packed FP64 triangle SA and
 // x in SX. Rows 32 .. N-1 of an order N <= 48 go to both half-warps, lane l
 // summing columns [0, N/2) (l < 16) or [N/2, N) (l >= 16) of row 32 + l % 16.
+// Each row sums in two halves (columns below and above N/2) interleaved with
+// the other row's chain: a single warp then keeps the FP64 pipe busy, where
+// one chain of dependent FMAs waits out the pipe's latency at every step.
 template <int N>
 __device__ __forceinline__ void residual(int lane, const double *SA, const double *SX,
                                          const double (&b)[(N + 31) / 32],
                                          double (&acc)[(N + 31) / 32])
 {
     constexpr int NR = (N + 31) / 32;
-    {
-        const int i = min(lane, N - 1); // lanes past N (N < 32) compute a row they discard
-        const int ci = pk_col(N, i) - i;
-        double s = b[0];
-#pragma unroll 4
-        for (int j = 0; j < N; ++j)
-            s = fma(-SA[j <= i ? pk_col(N, j) - j + i : ci + j], SX[j], s);
-        acc[0] = s;
+    constexpr int H = N / 2;
+    static_assert(N % 2 == 0, "an even order");
+    const int i0 = min(lane, N - 1); // lanes past N (N < 32) compute a row they discard
+    const double *lo0 = SA + i0, *hi0 = SA + pk_col(N, i0) - i0;
+    double s0 = b[0], s0h = 0.0;
+    if constexpr (NR == 1) {
+#pragma unroll
+        for (int t = 0; t < H; ++t) {
+            s0 = fma(-tri_at<N>(lo0, hi0, i0, t), SX[t], s0);
+            s0h = fma(-tri_at<N>(lo0, hi0, i0, H + t), SX[H + t], s0h);
+        }
+        acc[0] = s0 + s0h;
     }
-    if constexpr (NR == 2) {
-        if constexpr (N <= 48) {
-            constexpr int H = N / 2;
-            static_assert(N % 2 == 0, "split rows need an even order");
-            const bool lo = lane < 16;
-            const int i = min(32 + (lane & 15), N - 1);
-            const int ci = pk_col(N, i) - i;
-            const int c0 = lo ? 0 : H;
-            double s = lo ? b[1] : 0.0;
-#pragma unroll 4
-            for (int t = 0; t < H; ++t) {
-                // the first half's columns all lie left of the row (t < H <= 32 <= i)
-                const int j = c0 + t;
-                const int off = lo ? pk_col(N, t) - t + i
-                                   : (H + t <= i ? pk_col(N, H + t) - (H + t) + i : ci + j);
-                s = fma(-SA[off], SX[j], s);
-            }
-            acc[1] = s + __shfl_xor_sync(FULL, s, 16);
+    else if constexpr (N <= 48) {
+        const bool lower = lane < 16;
+        const int i1 = min(32 + (lane & 15), N - 1);
+        // lower half: columns t < H <= 32 <= i1, all in row i1's own part;
+        // upper half: columns H + t
+        const double *lo1 = SA + i1, *hi1 = SA + pk_col(N, i1) - i1;
+        const double *X1 = SX + (lower ? 0 : H);
+        double s1 = lower ? b[1] : 0.0;
+#pragma unroll
+        for (int t = 0; t < H; ++t) {
+            s0 = fma(-tri_at<N>(lo0, hi0, i0, t), SX[t], s0);
+            s0h = fma(-tri_at<N>(lo0, hi0, i0, H + t), SX[H + t], s0h);
+            double a;
+            if (lower)
+                a = lo1[pk_col(N, t) - t];
+            else
+                a = tri_at<N>(lo1, hi1, i1, H + t);
+            s1 = fma(-a, X1[t], s1);
         }
-        else {
-            const int i = min(lane + 32, N - 1);
-            const int ci = pk_col(N, i) - i;
-            double s = b[1];
-#pragma unroll 4
-            for (int j = 0; j < N; ++j)
-                s = fma(-SA[j <= i ? pk_col(N, j) - j + i : ci + j], SX[j], s);
-            acc[1] = s;
+        acc[0] = s0 + s0h;
+        acc[1] = s1 + __shfl_xor_sync(FULL, s1, 16);
+    }
+    else {
+        const int i1 = min(lane + 32, N - 1);
+        const double *lo1 = SA + i1, *hi1 = SA + pk_col(N, i1) - i1;
+        double s1 = b[1], s1h = 0.0;
+#pragma unroll
+        for (int t = 0; t < H; ++t) {
+            s0 = fma(-tri_at<N>(lo0, hi0, i0, t), SX[t], s0);
+            s1 = fma(-tri_at<N>(lo1, hi1, i1, t), SX[t], s1);
+            s0h = fma(-tri_at<N>(lo0, hi0, i0, H + t), SX[H + t], s0h);
+            s1h = fma(-tri_at<N>(lo1, hi1, i1, H + t), SX[H + t], s1h);
         }
+        acc[0] = s0 + s0h;
+        acc[1] = s1 + s1h;
     }
 }
 
@@ -341,21 +370,31 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         const long mw = have ? m0 + w : nlanes - 1;
         const long gw = mw / V;
         const double *bw = ap + gw * sa + (mw - gw * V);
-        double *Sw = SAall + w * PKS;
+        // element (j + rr + 32 s, j): its source steps by si + sj and its
+        // packed index by N - j from one column to the next
+        constexpr int NS = (N + 31) / 32;
+        const double *src[NS];
+        int dst[NS];
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            src[q] = bw + (long)(rr + 32 * q) * A0.si;
+            dst[q] = w * PKS + rr + 32 * q;
+        }
+        const long step = A0.si + A0.sj;
 #pragma unroll 1
         for (int j = 0; j < N; ++j) {
-            const double *colp = bw + (long)j * A0.sj;
-            double *Sj = Sw + pk_col(N, j) - j;
             const bool jn = have && j < n;
 #pragma unroll
-            for (int s = 0; s < (N + 31) / 32; ++s) {
-                const int i = j + rr + 32 * s;
+            for (int q = 0; q < NS; ++q) {
+                const int i = j + rr + 32 * q;
                 if (i < N) {
                     if (jn && i < n)
-                        cp_async8(Sj + i, colp + (long)i * A0.si);
+                        cp_async8(SAall + dst[q], src[q]);
                     else
-                        Sj[i] = (i == j) ? 1.0 : 0.0;
+                        SAall[dst[q]] = (i == j) ? 1.0 : 0.0;
                 }
+                src[q] += step;
+                dst[q] += N - j;
             }
         }
         cp_async_wait_all();
