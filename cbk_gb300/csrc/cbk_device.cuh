@@ -70,6 +70,11 @@ __device__ __forceinline__ bool lane_of(long ngroups, int V, Lane &ln)
 
 template <typename T> __device__ __forceinline__ T rcp(T x) { return T(1) / x; }
 
+template <typename T> __host__ __device__ constexpr T FLT_OR_DBL_MAX()
+{
+    return sizeof(T) == 8 ? T(1.7976931348623157e308) : T(3.40282347e38f);
+}
+
 // max(a, b) that keeps a NaN (fmaxf drops it): a NaN residual norm must stop
 // a refinement rather than pass its convergence test
 __device__ __forceinline__ float fmax_nan(float a, float b)
@@ -217,7 +222,14 @@ template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int
 {
     for (int j = j0; j < j1; ++j) {
         const T a = A(j, j);
-        const T inva = rcp(a);
+        T inva;
+        if (!LDLT && a > T(0) && a <= FLT_OR_DBL_MAX<T>()) {
+            const T r = rsqrt(a);
+            inva = r * r;
+        }
+        else {
+            inva = rcp(a);
+        }
         switch (j1 - j - 1) {
         case 7: rank1_panel<T, 7>(n, A, j, inva); break;
         case 6: rank1_panel<T, 6>(n, A, j, inva); break;
@@ -232,7 +244,16 @@ template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int
         if (LDLT) {
             scale = inva; // D(j) = a stays on the diagonal
         }
-        else {
+        else if (a > T(0) && a <= FLT_OR_DBL_MAX<T>()) {
+            // r = 1/sqrt(a): then 1/a = r^2, sqrt(a) = a r and the column
+            // scale sqrt(a)/a = r -- one reciprocal square root where the
+            // reciprocal and the square root each take several FP64-pipe
+            // passes (a few ulps apart from the separate operations)
+            const T r = rsqrt(a);
+            A(j, j) = a * r;
+            scale = r;
+        }
+        else { // zero, negative, infinite or NaN pivot: the plain operations
             const T d = sqrt(a);
             A(j, j) = d;
             scale = d * inva;
@@ -261,8 +282,13 @@ template <typename T, bool LDLT> __device__ void factor_lane(int n, LV<T> A)
 // into the backward sweep's first touch of each row
 // (src/cbk_sytrsnp_compact.hpp:51-78); otherwise each row is scaled by
 // 1/L(i,i) (src/cbk_potrs_compact.hpp:46-58).
+// 1/L(i,i) of the first RINV rows is computed once per lane (sym_solve_lane)
+// and shared by both sweeps and every block of right-hand sides; rows past it
+// recompute it.
+constexpr int RINV = 64;
+
 template <typename T, bool UNIT, int NB>
-__device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0)
+__device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0, const T *rinv)
 {
     for (int i = 0; i < n; ++i) {
         T w[NB];
@@ -281,7 +307,7 @@ __device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0)
                 B(i, c0 + c) = w[c];
         }
         else {
-            const T r = rcp(L(i, i));
+            const T r = i < RINV ? rinv[i] : rcp(L(i, i));
 #pragma unroll
             for (int c = 0; c < NB; ++c)
                 B(i, c0 + c) = w[c] * r;
@@ -289,7 +315,7 @@ __device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0)
     }
     for (int i = n - 1; i >= 0; --i) {
         T w[NB];
-        const T r = rcp(L(i, i));
+        const T r = i < RINV ? rinv[i] : rcp(L(i, i));
 #pragma unroll
         for (int c = 0; c < NB; ++c)
             w[c] = UNIT ? B(i, c0 + c) * r : B(i, c0 + c);
@@ -307,14 +333,18 @@ __device__ void sym_solve_block(int n, LV<T> L, LV<T> B, int c0)
 
 template <typename T, bool UNIT> __device__ void sym_solve_lane(int n, int nrhs, LV<T> L, LV<T> B)
 {
+    T rinv[RINV];
+    const int nr = n < RINV ? n : RINV;
+    for (int i = 0; i < nr; ++i)
+        rinv[i] = rcp(L(i, i));
     int c0 = 0;
     for (; c0 + 4 <= nrhs; c0 += 4)
-        sym_solve_block<T, UNIT, 4>(n, L, B, c0);
+        sym_solve_block<T, UNIT, 4>(n, L, B, c0, rinv);
     if (nrhs - c0 >= 2) {
-        sym_solve_block<T, UNIT, 2>(n, L, B, c0);
+        sym_solve_block<T, UNIT, 2>(n, L, B, c0, rinv);
         c0 += 2;
     }
-    if (nrhs - c0 >= 1) sym_solve_block<T, UNIT, 1>(n, L, B, c0);
+    if (nrhs - c0 >= 1) sym_solve_block<T, UNIT, 1>(n, L, B, c0, rinv);
 }
 
 // ---------------------------------------------------------------------

@@ -313,10 +313,13 @@ __global__ void __launch_bounds__(128, 4)
             s += fabsf(W(j, i));
         anorm = fmaxf(anorm, s);
     }
+    float rinv[RINV]; // 1/L(i,i) of the FP32 factor, for every solve below
     if (status == 0) {
         factor_lane<float, false>(n, W);
         for (int i = 0; i < n; ++i)
             if (!(W(i, i) > 0.f)) status = -1;
+        for (int i = 0; i < RINV && i < n; ++i)
+            rinv[i] = rcp(W(i, i));
     }
     // the norms, the stopping test and the reported backward error are FP32
     // (they only steer the iteration); the FP64 pipe does the residual and x
@@ -330,7 +333,7 @@ __global__ void __launch_bounds__(128, 4)
             bnorm = fmaxf(bnorm, fabsf(b));
             Z[(long)i * V] = b;
         }
-        sym_solve_block<float, false, 1>(n, W, Zv, 0);
+        sym_solve_block<float, false, 1>(n, W, Zv, 0, rinv);
         float xnorm = 0.f;
         for (int i = 0; i < n; ++i) {
             const float z = Z[(long)i * V];
@@ -360,7 +363,7 @@ __global__ void __launch_bounds__(128, 4)
                 break;
             }
             rprev = rnorm;
-            sym_solve_block<float, false, 1>(n, W, Zv, 0);
+            sym_solve_block<float, false, 1>(n, W, Zv, 0, rinv);
             xnorm = 0.f;
             for (int i = 0; i < n; ++i) {
                 const double xi = X[(long)i * V] + (double)Z[(long)i * V];
