@@ -511,7 +511,8 @@ def e2e(args, cbk, batches, barrier, ws):
                                            dtype=torch.uint8, device=b["ap0"].device)))
     del b
     groups = (NM + V - 1) // V
-    h2d = sum(groups * V * 8 * (h["n"] * h["n"] + h["n"] * NRHS) for h in host)
+    # pinned A: the library reads only its lower triangle over the host link
+    h2d = sum(groups * V * 8 * (h["n"] * (h["n"] + 1) // 2 + h["n"] * NRHS) for h in host)
     d2h = sum(groups * V * 8 * h["n"] * NRHS for h in host)
 
     def one():
@@ -536,9 +537,9 @@ def e2e(args, cbk, batches, barrier, ws):
     t = slowest_rank([sum(ts) / len(ts)], batches[0]["ap"].device)[0]
     return {"value": job_throughput(NM * len(SIZES), t, ws), "unit": UNIT, "ms_per_step": t,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "path": "cbk_cuda_dposv_refined_compact_host per n: pinned host A and b in, x "
-                    "out, contiguous copies per chunk pipelined with the solves in 3 device "
-                    "slots; host wall clock around the four calls"}
+            "path": "cbk_cuda_dposv_refined_compact_host per n: pinned host A (its lower "
+                    "triangle, read by the device) and b in, x out, pipelined with the solves "
+                    "in 3 device slots; host wall clock around the four calls"}
 
 
 # ---------------------------------------------------------------------------

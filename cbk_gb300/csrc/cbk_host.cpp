@@ -6,14 +6,17 @@
 // nothing because its kernels run on the CPU). Here a host batch is cut into
 // chunks of whole groups that flow through NBUF device slots, each slot on its
 // own stream: while one chunk is solved, the next one is copied in and the
-// previous one out, so the time is close to that of the copies alone. A
-// chunk's groups are contiguous in the compact layout, so each of its arrays
-// moves as one contiguous copy: on a GB300 host link that runs at the link's
-// full rate, while 2-D copies of only the referenced triangle (half of A's
-// bytes) measured three times slower. B (X) is copied back; A is copied back
-// only for a chunk in which some lane fell back to the FP64 path (those lanes
-// then hold the FP64 factor, the others the unchanged input), so the results
-// in host memory are exactly the device entry point's.
+// previous one out, so the time is close to that of the copies alone.
+// When A is in pinned host memory the device reads it directly: a kernel
+// gathers only the referenced triangle (half of A's bytes) over the host link,
+// which its 16-byte loads of whole contiguous runs drive at the link's full
+// rate (2-D copies of the same runs by the copy engine measured three times
+// slower). Otherwise (pageable memory) a chunk's groups, contiguous in the
+// compact layout, move as one copy. B moves as one contiguous copy each way.
+// A goes back to the host only for a chunk in which some lane fell back to
+// the FP64 path (those lanes then hold the FP64 factor, the others the
+// unchanged input) -- by the same triangle kernel when A is pinned -- so the
+// results in host memory are exactly the device entry point's.
 #include "cbk_launch.h"
 
 #include <algorithm>
@@ -71,6 +74,16 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
     const Plan p = plan(row, n, nrhs, ldap, ldbp, V, nm);
     char *const ha = reinterpret_cast<char *>(ap);
     char *const hb = reinterpret_cast<char *>(bp);
+    // pinned (or registered) A: the device address the triangle kernel reads
+    double *zc = nullptr;
+    {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, ap) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+            at.devicePointer != nullptr)
+            zc = static_cast<double *>(at.devicePointer);
+        cudaGetLastError(); // a pageable pointer is not an error
+    }
+    const size_t ga_doubles = p.ga / sizeof(double);
 
     struct Slot {
         cudaStream_t s = nullptr;
@@ -111,8 +124,12 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         int fell = 0;
         if (keep(cudaMemcpyAsync(&fell, sl.cnt, sizeof(int), cudaMemcpyDeviceToHost, sl.s)) &&
             keep(cudaStreamSynchronize(sl.s)) && fell > 0) {
-            keep(cudaMemcpyAsync(ha + (size_t)sl.g0 * p.ga, sl.a, (size_t)sl.groups * p.ga,
-                                 cudaMemcpyDeviceToHost, sl.s));
+            if (zc)
+                keep(launch_tri_copy(row, up, n, ldap, V, sl.groups, sl.a,
+                                     zc + (size_t)sl.g0 * ga_doubles, sl.s));
+            else
+                keep(cudaMemcpyAsync(ha + (size_t)sl.g0 * p.ga, sl.a, (size_t)sl.groups * p.ga,
+                                     cudaMemcpyDeviceToHost, sl.s));
             keep(cudaStreamSynchronize(sl.s));
         }
         sl.g0 = -1;
@@ -126,8 +143,12 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         const long lane0 = g0 * V;
         const int nmc = (int)std::min((long)nm - lane0, groups * V);
         keep(cudaMemsetAsync(sl.cnt, 0, sizeof(int), sl.s));
-        keep(cudaMemcpyAsync(sl.a, ha + (size_t)g0 * p.ga, (size_t)groups * p.ga,
-                             cudaMemcpyHostToDevice, sl.s));
+        if (zc)
+            keep(launch_tri_copy(row, up, n, ldap, V, groups, zc + (size_t)g0 * ga_doubles, sl.a,
+                                 sl.s));
+        else
+            keep(cudaMemcpyAsync(sl.a, ha + (size_t)g0 * p.ga, (size_t)groups * p.ga,
+                                 cudaMemcpyHostToDevice, sl.s));
         keep(cudaMemcpyAsync(sl.b, hb + (size_t)g0 * p.gb, (size_t)groups * p.gb,
                              cudaMemcpyHostToDevice, sl.s));
         keep(launch_posv_refined(row, up, n, nrhs, sl.a, ldap, sl.b, ldbp, V, nmc, max_iter, sl.it,

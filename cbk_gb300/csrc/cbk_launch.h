@@ -109,6 +109,11 @@ size_t posv_refined_host_lwork(bool row, int n, int nrhs, int ldap, int ldbp, in
 cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
                               int ldbp, int V, int nm, int max_iter, int *iters, double *berr,
                               void *dwork, cudaStream_t caller);
+// the referenced triangle of `groups` compact groups of n x n matrices
+// (leading dimension ld, group stride ld n V), src -> dst in place
+// (cbk_kernels_pack.cu); either pointer may be device-addressable host memory
+cudaError_t launch_tri_copy(bool row, bool up, int n, int ld, int V, long groups,
+                            const double *src, double *dst, cudaStream_t s);
 // *count += the number of negative entries of iters[0 .. n)
 cudaError_t launch_count_negative(const int *iters, int n, int *count, cudaStream_t s);
 

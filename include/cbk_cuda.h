@@ -256,8 +256,10 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
  * host, as in ?posv_compact (include/cbk.h:218-234) -- over the device solve
  * above. The batch is cut into chunks of whole groups that pass through
  * three device slots on three streams, so that copying one chunk in, solving
- * another and copying a third out overlap; each chunk's A and B move as one
- * contiguous copy each. B (X) is copied back; A is copied back only for a
+ * another and copying a third out overlap. When ap is pinned (or registered)
+ * host memory, the device reads only the referenced triangle of A from it
+ * directly; otherwise each chunk's A moves as one contiguous copy. B moves as
+ * one contiguous copy each way. B (X) is copied back; A is copied back only for a
  * chunk in which some lane fell back (ap then holds those lanes' FP64
  * factor), so ap, bp, iters and berr end exactly as the device entry point
  * leaves them. dwork is a device workspace of at least
