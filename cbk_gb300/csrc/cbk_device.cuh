@@ -75,6 +75,73 @@ template <typename T> __host__ __device__ constexpr T FLT_OR_DBL_MAX()
     return sizeof(T) == 8 ? T(1.7976931348623157e308) : T(3.40282347e38f);
 }
 
+// ---------------------------------------------------------------------
+// FP64 <-> FP32 on the integer pipe. On a GB300 a hardware conversion (and an
+// FP64 compare) takes a slot of the FP64 pipe -- the pipe the mixed-precision
+// solves are bound by -- so the refined kernels convert with bit operations.
+// ---------------------------------------------------------------------
+
+// FP64 -> FP32 toward zero on the integer pipe, times 2^shift (subnormal
+// results flushed, values beyond the FP32 range become infinities).
+__device__ __forceinline__ float d2f_rz(double a, int shift = 0)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const int fe = e - 1023 + 127 + shift;
+    unsigned bits;
+    if (e == 0x7ff)
+        bits = sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u | mant : 0u);
+    else if (e == 0 || fe <= 0)
+        bits = sign;
+    else if (fe >= 255)
+        bits = sign | 0x7f800000u;
+    else
+        bits = sign | ((unsigned)fe << 23) | mant;
+    return __uint_as_float(bits);
+}
+
+// The same for |a| < 2^128 (callers check the range apart): no branches.
+// Zeros, FP64 subnormals and results below the FP32 normal range give a
+// signed zero; a NaN gives some float (its residual stays NaN).
+__device__ __forceinline__ float d2f_rz_inrange(double a)
+{
+    const unsigned hi = (unsigned)__double2hiint(a), lo = (unsigned)__double2loint(a);
+    const int fe = (int)((hi >> 20) & 0x7ffu) - 896;
+    const unsigned bits =
+        (hi & 0x80000000u) | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(fe > 0 ? bits : hi & 0x80000000u);
+}
+
+// FP32 -> FP64 times 2^shift on the integer pipe (exact; FP32 subnormals
+// flushed to zero)
+__device__ __forceinline__ double f2d_int(float f, int shift = 0)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u;
+    const int e = (int)((u >> 23) & 0xffu);
+    const unsigned mant = u & 0x7fffffu;
+    unsigned hi;
+    if (e == 0)
+        return __hiloint2double((int)sign, 0);
+    if (e == 0xff)
+        hi = sign | 0x7ff00000u | (mant >> 3) | (mant ? 0x80000u : 0u);
+    else
+        hi = sign | ((unsigned)(e - 127 + 1023 + shift) << 20) | (mant >> 3);
+    return __hiloint2double((int)hi, (int)(mant << 29));
+}
+
+// |a| > FLT_MAX, infinities included and NaN not (LAPACK dlag2s's test), on
+// the 32-bit halves of a
+__device__ __forceinline__ bool beyond_fp32(double a)
+{
+    const unsigned ah = (unsigned)__double2hiint(a) & 0x7fffffffu, lo = (unsigned)__double2loint(a);
+    const bool big = ah > 0x47efffffu || (ah == 0x47efffffu && lo > 0xe0000000u);
+    const bool nan = ah > 0x7ff00000u || (ah == 0x7ff00000u && lo != 0u);
+    return big && !nan;
+}
+
 // max(a, b) that keeps a NaN (fmaxf drops it): a NaN residual norm must stop
 // a refinement rather than pass its convergence test
 __device__ __forceinline__ float fmax_nan(float a, float b)

@@ -55,9 +55,16 @@ __host__ __device__ constexpr int tix(int i, int j, int N)
     return j * (2 * N - j + 1) / 2 + (i - j);
 }
 
-__device__ __forceinline__ bool fits_fp32(double a)
+
+// The exact FP32-range test of the lower triangle (the rare path after a
+// quick screen; not inlined, so that it takes no registers from the caller).
+__device__ __noinline__ bool any_beyond_fp32(int n, LV<double> A)
 {
-    return !(fabs(a) > (double)FLT_MAX); // NaN passes: garbage in, garbage out
+    bool any = false;
+    for (int j = 0; j < n; ++j)
+        for (int i = j; i < n; ++i)
+            any |= beyond_fp32(A(i, j));
+    return any;
 }
 
 struct RefineOut {
@@ -127,9 +134,12 @@ __global__ void __launch_bounds__(128)
     if (up) A = A.t();
     const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
 
+    // FP64 <-> FP32 conversions and range tests are integer operations here:
+    // a hardware conversion or FP64 compare takes an FP64-pipe slot
     float L[N * (N + 1) / 2];
     float rs[N];
     int status = 0;
+    unsigned hmax = 0; // largest high word of |a|: a quick screen for the FP32 range
 #pragma unroll
     for (int i = 0; i < N; ++i)
         rs[i] = 0.f;
@@ -138,12 +148,13 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int i = j; i < N; ++i) {
             const double a = A(i, j);
-            if (!fits_fp32(a)) status = -2;
-            const float f = (float)a;
+            hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
+            const float f = d2f_rz_inrange(a);
             L[tix(i, j, N)] = f;
             rs[i] += fabsf(f);
             if (i != j) rs[j] += fabsf(f);
         }
+    if (hmax >= 0x47efffffu && any_beyond_fp32(N, A)) status = -2;
     float anorm = 0.f;
 #pragma unroll
     for (int i = 0; i < N; ++i)
@@ -169,24 +180,25 @@ __global__ void __launch_bounds__(128)
     // every quantity that only steers the iteration (norms, the stopping test,
     // the reported backward error) is kept in FP32: the FP64 pipe is left to
     // the residual itself and the FP64 update of x
+    // LAPACK dsposv's test ||r|| <= sqrt(n) eps64 ||A|| ||x||, in FP32 while
+    // the right side is a normal FP32 number, in FP64 below that
     const double cte = (double)anorm * EPS64 * sqrt((double)N);
+    const float cte32 = (float)cte;
     int it_max = 0, col = 0;
     float worst = 0.f;
     for (; col < nrhs && status == 0; ++col) {
         double x[N];
-        float z[N], x32[N];
+        float z[N];
         float bnorm = 0.f;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-            z[i] = (float)B(i, col);
+            z[i] = d2f_rz(B(i, col));
             bnorm = fmaxf(bnorm, fabsf(z[i]));
         }
         solve32<N>(L, rinv, z);
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
-            x[i] = (double)z[i];
-            x32[i] = z[i];
-        }
+        for (int i = 0; i < N; ++i)
+            x[i] = f2d_int(z[i]);
         float rprev = INFINITY;
         for (int it = 0;; ++it) {
             // opaque strides: the n^2 addresses of A are recomputed each step
@@ -200,11 +212,12 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
                 for (int j = 0; j < N; ++j)
                     acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
-                z[i] = (float)acc;
+                z[i] = d2f_rz(acc);
                 rnorm = fmax_nan(rnorm, fabsf(z[i]));
-                xnorm = fmaxf(xnorm, fabsf(x32[i]));
+                xnorm = fmaxf(xnorm, fabsf(d2f_rz_inrange(x[i])));
             }
-            if ((double)rnorm <= cte * (double)xnorm) {
+            const float thr = cte32 * xnorm;
+            if (thr >= 0x1p-100f ? rnorm <= thr : (double)rnorm <= cte * (double)xnorm) {
                 const float den = anorm * xnorm + bnorm;
                 worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
                 it_max = max(it_max, it);
@@ -217,10 +230,8 @@ __global__ void __launch_bounds__(128)
             rprev = rnorm;
             solve32<N>(L, rinv, z);
 #pragma unroll
-            for (int i = 0; i < N; ++i) {
-                x[i] += (double)z[i];
-                x32[i] += z[i];
-            }
+            for (int i = 0; i < N; ++i)
+                x[i] += f2d_int(z[i]);
         }
         if (status == 0) {
 #pragma unroll
@@ -275,7 +286,7 @@ __device__ __forceinline__ void resid_rows(int n, int i0, int col, LV<double> A,
     }
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
-        const float z = (float)acc[r];
+        const float z = d2f_rz(acc[r]);
         Z[(long)(i0 + r) * V] = z;
         rnorm = fmax_nan(rnorm, fabsf(z));
     }
@@ -301,8 +312,8 @@ __global__ void __launch_bounds__(128, 4)
     for (int j = 0; j < n; ++j)
         for (int i = j; i < n; ++i) {
             const double a = A(i, j);
-            if (!fits_fp32(a)) status = -2;
-            W(i, j) = (float)a;
+            if (beyond_fp32(a)) status = -2;
+            W(i, j) = d2f_rz_inrange(a);
         }
     float anorm = 0.f;
     for (int i = 0; i < n; ++i) {
@@ -329,7 +340,7 @@ __global__ void __launch_bounds__(128, 4)
     for (; col < nrhs && status == 0; ++col) {
         float bnorm = 0.f;
         for (int i = 0; i < n; ++i) {
-            const float b = (float)B(i, col);
+            const float b = d2f_rz(B(i, col));
             bnorm = fmaxf(bnorm, fabsf(b));
             Z[(long)i * V] = b;
         }
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(128, 4)
         float xnorm = 0.f;
         for (int i = 0; i < n; ++i) {
             const float z = Z[(long)i * V];
-            X[(long)i * V] = (double)z;
+            X[(long)i * V] = f2d_int(z);
             xnorm = fmaxf(xnorm, fabsf(z));
         }
         float rprev = INFINITY;
@@ -352,7 +363,8 @@ __global__ void __launch_bounds__(128, 4)
             case 1: resid_rows<1>(n, i0, col, A, B, X, Z, V, rnorm); break;
             default: break;
             }
-            if ((double)rnorm <= cte * (double)xnorm) {
+            const float thr = (float)cte * xnorm;
+            if (thr >= 0x1p-100f ? rnorm <= thr : (double)rnorm <= cte * (double)xnorm) {
                 const float den = anorm * xnorm + bnorm;
                 worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
                 it_max = max(it_max, it);
@@ -366,9 +378,9 @@ __global__ void __launch_bounds__(128, 4)
             sym_solve_block<float, false, 1>(n, W, Zv, 0, rinv);
             xnorm = 0.f;
             for (int i = 0; i < n; ++i) {
-                const double xi = X[(long)i * V] + (double)Z[(long)i * V];
+                const double xi = X[(long)i * V] + f2d_int(Z[(long)i * V]);
                 X[(long)i * V] = xi;
-                xnorm = fmaxf(xnorm, fabsf((float)xi));
+                xnorm = fmaxf(xnorm, fabsf(d2f_rz(xi)));
             }
         }
         if (status == 0)
