@@ -461,9 +461,12 @@ def run_gpu(args):
         "per_n": per_n,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
-                     "kernel": f"k_posv_refined (n={ndom})",
+                     "binding": "the FP64 pipe, not HBM (see fp64_pipe)",
+                     "kernel": f"k_posv_refined_warp<{ndom}> (n={ndom})" if 16 < ndom <= 64
+                     else f"k_posv_refined (n={ndom})",
                      "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)"},
-        "fp64_pipe": {"kernel": f"k_posv_refined (n={ndom})", "unit": "TFLOP/s",
+        "fp64_pipe": {"kernel": f"k_posv_refined_warp<{ndom}> (n={ndom})" if 16 < ndom <= 64
+                      else f"k_posv_refined (n={ndom})", "unit": "TFLOP/s",
                       "achieved": fp64_flops / (dom_ms * 1e-3) / 1e12,
                       "plain_achieved": NM * plain_flops(ndom) / (pl_dom_ms * 1e-3) / 1e12,
                       "peak": rate, "peak_source": "measured FP64 FMA rate "
@@ -526,16 +529,23 @@ def e2e(args, cbk, batches, barrier, ws):
             info = cbk.dposv_refined_compact_host("C", "L", h["n"], NRHS, h["ap"], h["n"], h["bp"],
                                                   h["n"], V, NM, 10, None, None, h["dwork"])
             assert info == 0, info
+            h["t"] = time.perf_counter()
         torch.cuda.synchronize()
         t = (time.perf_counter() - t0) * 1e3
         barrier()
+        per.append([(h["t"] - (host[k - 1]["t"] if k else t0)) * 1e3 for k, h in enumerate(host)])
         return t
+
+    per = []
 
     for _ in range(max(1, args.warmup // 2)):
         one()
     ts = [one() for _ in range(args.steps)]
     t = slowest_rank([sum(ts) / len(ts)], batches[0]["ap"].device)[0]
+    per = per[-len(ts):]
+    per_n_ms = {str(h["n"]): statistics.mean(p[k] for p in per) for k, h in enumerate(host)}
     return {"value": job_throughput(NM * len(SIZES), t, ws), "unit": UNIT, "ms_per_step": t,
+            "per_n_ms": per_n_ms,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "path": "cbk_cuda_dposv_refined_compact_host per n: pinned host A (its lower "
                     "triangle, read by the device) and b in, x out, pipelined with the solves "
