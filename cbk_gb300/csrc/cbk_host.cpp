@@ -87,6 +87,7 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
 
     struct Slot {
         cudaStream_t s = nullptr;
+        cudaEvent_t ready = nullptr; // the chunk's inputs are in the slot
         double *a, *b, *be;
         int *it, *cnt;
         void *ws;
@@ -109,11 +110,23 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         if (err == cudaSuccess && e != cudaSuccess) err = e;
         return err == cudaSuccess;
     };
-    // the slots' streams start after the caller's prior work on its stream
+    // The inputs move on one stream of the highest priority, the solves and
+    // the outputs on one stream per slot: a solve launched first would
+    // otherwise keep the GPU until its last block is dispatched, and the copy
+    // of the next chunk (a persistent kernel) must get the resources its
+    // blocks free. All streams start after the caller's prior work on its
+    // stream.
+    cudaStream_t in = nullptr;
+    int lo_prio = 0, hi_prio = 0;
+    keep(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     keep(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
     if (err == cudaSuccess) keep(cudaEventRecord(start, caller));
+    if (err == cudaSuccess &&
+        keep(cudaStreamCreateWithPriority(&in, cudaStreamNonBlocking, hi_prio)))
+        keep(cudaStreamWaitEvent(in, start, 0));
     for (int k = 0; k < NBUF && err == cudaSuccess; ++k)
-        if (keep(cudaStreamCreateWithFlags(&slot[k].s, cudaStreamNonBlocking)))
+        if (keep(cudaStreamCreateWithFlags(&slot[k].s, cudaStreamNonBlocking)) &&
+            keep(cudaEventCreateWithFlags(&slot[k].ready, cudaEventDisableTiming)))
             keep(cudaStreamWaitEvent(slot[k].s, start, 0));
 
     // a chunk is finished once its stream is idle; if one of its lanes fell
@@ -142,15 +155,18 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         const long groups = std::min(p.chunk, p.ngroups - g0);
         const long lane0 = g0 * V;
         const int nmc = (int)std::min((long)nm - lane0, groups * V);
-        keep(cudaMemsetAsync(sl.cnt, 0, sizeof(int), sl.s));
+        // the slot is idle (finish), so its inputs may be overwritten now
+        keep(cudaMemsetAsync(sl.cnt, 0, sizeof(int), in));
         if (zc)
             keep(launch_tri_copy(row, up, n, ldap, V, groups, zc + (size_t)g0 * ga_doubles, sl.a,
-                                 sl.s));
+                                 in));
         else
             keep(cudaMemcpyAsync(sl.a, ha + (size_t)g0 * p.ga, (size_t)groups * p.ga,
-                                 cudaMemcpyHostToDevice, sl.s));
+                                 cudaMemcpyHostToDevice, in));
         keep(cudaMemcpyAsync(sl.b, hb + (size_t)g0 * p.gb, (size_t)groups * p.gb,
-                             cudaMemcpyHostToDevice, sl.s));
+                             cudaMemcpyHostToDevice, in));
+        keep(cudaEventRecord(sl.ready, in));
+        keep(cudaStreamWaitEvent(sl.s, sl.ready, 0));
         keep(launch_posv_refined(row, up, n, nrhs, sl.a, ldap, sl.b, ldbp, V, nmc, max_iter, sl.it,
                                  berr ? sl.be : nullptr, sl.ws, sl.s));
         keep(launch_count_negative(sl.it, nmc, sl.cnt, sl.s));
@@ -167,11 +183,17 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
     }
     for (int k = 0; k < NBUF; ++k)
         if (err == cudaSuccess) finish(slot[k]);
-    for (int k = 0; k < NBUF; ++k)
+    if (in) {
+        cudaStreamSynchronize(in);
+        cudaStreamDestroy(in);
+    }
+    for (int k = 0; k < NBUF; ++k) {
         if (slot[k].s) {
             cudaStreamSynchronize(slot[k].s);
             cudaStreamDestroy(slot[k].s);
         }
+        if (slot[k].ready) cudaEventDestroy(slot[k].ready);
+    }
     if (start) cudaEventDestroy(start);
     return err;
 }

@@ -14,6 +14,8 @@
 #include "cbk_device.cuh"
 #include "cbk_launch.h"
 
+#include <algorithm>
+
 namespace cbkcuda {
 
 namespace {
@@ -144,19 +146,24 @@ PackGeom make_geom(bool row, int m, int n, int lda, long long stride, int ldap, 
 // block copies it with 16-byte moves; dst has src's layout. Either side may
 // be host memory the device can address (pinned): the copy then runs over the
 // host link at its full rate with half the bytes of the whole matrices.
-__global__ void k_tri_copy(const double *__restrict__ src, double *__restrict__ dst,
-                           bool from_diag, int n, int ld, int V, long groups, long gstride)
+// The grid is persistent -- two blocks per SM striding over the runs -- so
+// that the copy keeps running beside a solve that fills the rest of the GPU
+// (a grid of one block per run would wait for the solve's blocks to drain).
+__global__ void __launch_bounds__(256)
+    k_tri_copy(const double *__restrict__ src, double *__restrict__ dst, bool from_diag, int n,
+               int ld, int V, long groups, long gstride)
 {
-    const long b = blockIdx.x;
-    const long g = b / n;
-    const int k = (int)(b - g * n);
-    if (g >= groups) return;
-    const long start = ((long)k * ld + (from_diag ? k : 0)) * V;
-    const long len2 = (long)(from_diag ? n - k : k + 1) * V / 2; // V is even
-    const double2 *s = reinterpret_cast<const double2 *>(src + g * gstride + start);
-    double2 *d = reinterpret_cast<double2 *>(dst + g * gstride + start);
-    for (long i = threadIdx.x; i < len2; i += blockDim.x)
-        d[i] = s[i];
+    const long runs = groups * n;
+    for (long b = blockIdx.x; b < runs; b += gridDim.x) {
+        const long g = b / n;
+        const int k = (int)(b - g * n);
+        const long start = ((long)k * ld + (from_diag ? k : 0)) * V;
+        const long len2 = (long)(from_diag ? n - k : k + 1) * V / 2; // V is even
+        const double2 *s = reinterpret_cast<const double2 *>(src + g * gstride + start);
+        double2 *d = reinterpret_cast<double2 *>(dst + g * gstride + start);
+        for (long i = threadIdx.x; i < len2; i += blockDim.x)
+            d[i] = s[i];
+    }
 }
 
 } // namespace
@@ -165,8 +172,11 @@ cudaError_t launch_tri_copy(bool row, bool up, int n, int ld, int V, long groups
                             const double *src, double *dst, cudaStream_t s)
 {
     if (groups <= 0 || n <= 0) return cudaSuccess;
-    const long blocks = groups * n;
-    k_tri_copy<<<(unsigned)blocks, 128, 0, s>>>(src, dst, row == up, n, ld, V, groups,
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long blocks = std::min<long>(groups * n, 2L * std::max(sms, 1));
+    k_tri_copy<<<(unsigned)blocks, 256, 0, s>>>(src, dst, row == up, n, ld, V, groups,
                                                 (long)ld * n * V);
     return cudaGetLastError();
 }
