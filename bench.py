@@ -314,6 +314,16 @@ def run_gpu(args):
         if ws > 1:
             dist.barrier()
 
+    # launch shapes from the library's autotuner, at this layout's width, for
+    # both paths (untimed setup; shapes never change results)
+    tuned = {}
+    if not args.no_tune:
+        for n in SIZES:
+            for routine in ("posv_refined", "posv"):
+                info, r = cbk.autotune_at(routine, "d", n, n, NRHS, NM, V)
+                assert info == 0, (routine, n, info)
+                tuned[f"{routine} n={n}"] = {"threads": r["threads"], "variant": r["variant"]}
+
     batches = []
     for n in SIZES:
         A, B = gen_batch(n, NM, gen, dev)
@@ -451,7 +461,8 @@ def run_gpu(args):
         "vs_baseline": None, "dtype": "f32 factor + f64 refinement (f64 results)", "data": DATA,
         "config": {"workload": WORKLOAD, "nm_per_n": NM, "n": list(SIZES), "nrhs": NRHS, "V": V,
                    "max_iter": 10, "l2": "flushed (256 MiB write) before every timed step",
-                   "inputs": "restored untimed before every step", "parallelism": "replicas"},
+                   "inputs": "restored untimed before every step", "parallelism": "replicas",
+                   "launch_shapes": tuned or "built-in defaults (--no-tune)"},
         "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": t_pl},
         "speedup_refined_vs_plain": plain_value and value / plain_value,
         "equal_error": {"bound": "berr <= 8 n eps64 (normwise, inf-norm)",
@@ -730,6 +741,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("cbk", "reference"), default="cbk")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the built-in launch shapes instead of autotuning them first")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5"), default="c3",

@@ -314,6 +314,20 @@ def autotune(routine: str, prec: str, m: int, n: int, nrhs: int, nm: int):
     return info, {"threads": r.threads, "variant": r.variant, "vlen": r.vlen, "ms": r.ms}
 
 
+def autotune_at(routine: str, prec: str, m: int, n: int, nrhs: int, nm: int, V: int):
+    """autotune at one interleave width V. Returns (info, dict)."""
+    import ctypes
+
+    from ._abi import lib
+    TR = _tr()
+    f = lib().cbk_cuda_autotune_at
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char_p, ctypes.c_char] + [ctypes.c_int] * 5 + [ctypes.POINTER(TR)]
+    r = TR()
+    info = f(routine.encode(), prec.encode(), m, n, nrhs, nm, V, ctypes.byref(r))
+    return info, {"threads": r.threads, "variant": r.variant, "vlen": r.vlen, "ms": r.ms}
+
+
 def tune_set(routine: str, prec: str, n: int, threads: int = 0, variant: int = 0,
              vlen: int = 0) -> int:
     import ctypes
@@ -364,4 +378,5 @@ def tune_load(path: str) -> int:
     return f(path.encode())
 
 
-__all__ += ["autotune", "tune_set", "tune_get", "tune_reset", "tune_save", "tune_load"]
+__all__ += ["autotune", "autotune_at", "tune_set", "tune_get", "tune_reset", "tune_save",
+            "tune_load"]

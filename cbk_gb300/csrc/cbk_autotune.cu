@@ -168,12 +168,15 @@ cudaError_t time_one(const Spec &sp, Batch<T> &B, cudaStream_t s, cudaEvent_t e0
 }
 
 template <typename T>
-int autotune(const Spec &sp, int m, int n, int nrhs, int nm, const cbk_cuda_tune_result &old,
-             cbk_cuda_tune_result *out)
+int autotune(const Spec &sp, int m, int n, int nrhs, int nm, int only_V,
+             const cbk_cuda_tune_result &old, cbk_cuda_tune_result *out)
 {
     constexpr int ds = sizeof(T);
     const bool warp = sp.kind == REFINED && posv_refined_warp_ok(n);
-    const int widths[] = {32, 64, 128};
+    const int all_widths[] = {32, 64, 128};
+    const int one_width[] = {only_V};
+    const int nwidths = only_V ? 1 : 3;
+    const int *widths = only_V ? one_width : all_widths;
     // the lane-per-matrix refined kernels are compiled for at most 128 threads
     const int lane_threads[] = {64, 128, 256}, refined_threads[] = {32, 64, 128};
     const int *threads = sp.kind == REFINED ? refined_threads : lane_threads;
@@ -185,7 +188,8 @@ int autotune(const Spec &sp, int m, int n, int nrhs, int nm, const cbk_cuda_tune
     if (!err) err = cudaEventCreate(&e1);
     float best = FLT_MAX;
     int best_shape = 0, best_V = 32;
-    for (int V : widths) {
+    for (int wi = 0; wi < nwidths; ++wi) {
+        const int V = widths[wi];
         if (err) break;
         Batch<T> B;
         err = make_batch<T>(sp, m, n, nrhs, V, nm, B, s);
@@ -229,8 +233,10 @@ int autotune(const Spec &sp, int m, int n, int nrhs, int nm, const cbk_cuda_tune
 
 using namespace cbkcuda;
 
-extern "C" int cbk_cuda_autotune(const char *routine, char prec, int m, int n, int nrhs, int nm,
-                                 cbk_cuda_tune_result *out)
+namespace {
+
+int autotune_entry(const char *routine, char prec, int m, int n, int nrhs, int nm, int only_V,
+                   cbk_cuda_tune_result *out)
 {
     const int r = routine_of(routine);
     if (r < 0) return -1;
@@ -261,6 +267,22 @@ extern "C" int cbk_cuda_autotune(const char *routine, char prec, int m, int n, i
     }
     cbk_cuda_tune_result old{};
     cbk_cuda_tune_get(routine, prec, sp.key, &old);
-    return prec == 'd' ? autotune<double>(sp, m, n, nrhs, nm, old, out)
-                       : autotune<float>(sp, m, n, nrhs, nm, old, out);
+    return prec == 'd' ? autotune<double>(sp, m, n, nrhs, nm, only_V, old, out)
+                       : autotune<float>(sp, m, n, nrhs, nm, only_V, old, out);
+}
+
+} // namespace
+
+extern "C" int cbk_cuda_autotune(const char *routine, char prec, int m, int n, int nrhs, int nm,
+                                 cbk_cuda_tune_result *out)
+{
+    return autotune_entry(routine, prec, m, n, nrhs, nm, 0, out);
+}
+
+extern "C" int cbk_cuda_autotune_at(const char *routine, char prec, int m, int n, int nrhs, int nm,
+                                    int V, cbk_cuda_tune_result *out)
+{
+    if (routine_of(routine) < 0) return -1;
+    if (V < 32 || V > 1024 || V % 32 != 0) return -7;
+    return autotune_entry(routine, prec, m, n, nrhs, nm, V, out);
 }

@@ -422,6 +422,10 @@ typedef struct {
 } cbk_cuda_tune_result;
 int cbk_cuda_autotune(const char *routine, char prec, int m, int n, int nrhs, int nm,
                       cbk_cuda_tune_result *out);
+/* The same at one interleave width V (a multiple of 32, -7 otherwise), for a
+ * caller whose layout is fixed. */
+int cbk_cuda_autotune_at(const char *routine, char prec, int m, int n, int nrhs, int nm, int V,
+                         cbk_cuda_tune_result *out);
 int cbk_cuda_tune_set(const char *routine, char prec, int n, int threads, int variant, int vlen);
 int cbk_cuda_tune_get(const char *routine, char prec, int n, cbk_cuda_tune_result *out);
 void cbk_cuda_tune_reset(void);

@@ -48,6 +48,8 @@ def test_argument_checks(tune):
     assert tune.autotune("posv", "d", 8, 8, 0, 64)[0] == -5
     assert tune.autotune("posv", "d", 8, 8, 1, 0)[0] == -6
     assert tune.autotune("posv_refined", "s", 8, 8, 1, 64)[0] == -2
+    assert tune.autotune_at("posv", "d", 8, 8, 1, 64, 48)[0] == -7
+    assert tune.autotune_at("nope", "d", 8, 8, 1, 64, 32)[0] == -1
 
 
 def test_save_load_round_trip(tune, tmp_path):
