@@ -118,7 +118,7 @@ __host__ __device__ constexpr int pk_stride(int N)
 template <int N, int WPB> constexpr size_t warp_smem_bytes()
 {
     return (size_t)WPB * ((size_t)pk_stride(N) * sizeof(double) + (size_t)2 * N * sizeof(double) +
-                          (size_t)3 * N * sizeof(float));
+                          (size_t)5 * N * sizeof(float));
 }
 
 struct WarpOut {
@@ -293,8 +293,8 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     double *const SB = SAall + WPB * (PKS + N) + warp * N; // b, the right-hand side being solved
     // the pivot column twice over (SC, 16-byte aligned: N is a multiple of 8)
     // and the vector of a matrix-vector product (SR)
-    float *const SC = reinterpret_cast<float *>(SAall + WPB * (PKS + 2 * N)) + warp * 3 * N;
-    float *const SR = SC + 2 * N;
+    float *const SC = reinterpret_cast<float *>(SAall + WPB * (PKS + 2 * N)) + warp * 5 * N;
+    float *const SR = SC + 4 * N;
 
     // ---- stage the block's matrices: packed lower triangles, identity past n ----
     // Thread t copies matrix t % WPB, rows t / WPB + 32 s of each column, with
@@ -441,31 +441,35 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     // the group every register index is static; the group ends by rotating
     // the registers by 8 (a split row passes 8 values across with shuffles).
     constexpr int U = 8;
-    static_assert(N % U == 0 && H % 4 == 0, "pivot groups and float4 columns");
+    static_assert(N % U == 0 && U % 2 == 0 && H % 4 == 0, "pivot groups, buffers, float4 columns");
     bool nonpos = false;
+    // The pivot column alternates between two buffers: a step writes the one
+    // the step before last read, which every lane finished before the last
+    // step's barrier -- so one barrier per step, and the next step's column
+    // can be written while this step's updates are still being issued.
 #pragma unroll 1
     for (int k0 = 0; k0 < N; k0 += U) {
-        // c[q] = column (k0 + q) mod N from the doubled column; the upper half
-        // of a split row reads from c[H] on
-        const float4 *C4 = reinterpret_cast<const float4 *>(SC + k0);
-        const float4 *CB4 =
-            reinterpret_cast<const float4 *>(SC + k0 + ((L::SPLIT && lane >= 16) ? H : 0));
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int k = k0 + u;
-            __syncwarp();
+            float *const S = (u & 1) ? SC + 2 * N : SC;
+            // c[q] = column (k0 + q) mod N from the doubled column; the upper
+            // half of a split row reads from c[H] on
+            const float4 *C4 = reinterpret_cast<const float4 *>(S + k0);
+            const float4 *CB4 =
+                reinterpret_cast<const float4 *>(S + k0 + ((L::SPLIT && lane >= 16) ? H : 0));
             if (N >= 32 || lane < N) {
-                SC[lane] = R0[u];
-                SC[lane + N] = R0[u];
+                S[lane] = R0[u];
+                S[lane + N] = R0[u];
             }
             if constexpr (L::TWO) {
                 if ((!L::SPLIT || lane < 16) && 32 + lane < N) {
-                    SC[32 + lane] = R1[u];
-                    SC[32 + lane + N] = R1[u];
+                    S[32 + lane] = R1[u];
+                    S[32 + lane + N] = R1[u];
                 }
             }
             __syncwarp();
-            const float p = SC[k];
+            const float p = S[k];
             nonpos |= !(p > 0.f);
             const float rp = rcp_approx(p);
             const bool own0 = lane == k;
