@@ -686,7 +686,7 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
     // four matrices per block (the staging loads then fill 32-byte sectors);
     // the order is padded to a multiple of 8, and the last template argument
     // caps the registers for the resident blocks wanted (measured: at n = 32
-    // six blocks beat five despite a few spills, at n = 48 four beat five).
+    // seven blocks beat six and five despite spills, at n = 48 four beat five).
     // Variant 1 asks for one block more per SM (fewer registers per thread).
     const bool more = variant_for(R_POSV_REFINED, n, 8) == 1;
 #define CBK_WARP(N, B)                                                                             \
@@ -694,7 +694,7 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
                 : launch_warp<N, 4, B>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s)
     switch ((n + 7) / 8) {
     case 3: CBK_WARP(24, 6);
-    case 4: CBK_WARP(32, 6);
+    case 4: CBK_WARP(32, 7);
     case 5: CBK_WARP(40, 4);
     case 6: CBK_WARP(48, 4);
     case 7: CBK_WARP(56, 3);
