@@ -296,6 +296,38 @@ def berr_max(A, X, B):
     return float((rn / (an * xn + bn)).max())
 
 
+def run_case(args):
+    """One small solve for a profiler to capture: the headline's batch for one
+    order (--case refined|plain N NM), solved twice (the second launch is the
+    one a capture skips to); prints a line, times nothing."""
+    import torch
+
+    import cbk_gb300 as cbk
+    kind, n, nm = args.case[0], int(args.case[1]), int(args.case[2])
+    if kind not in ("refined", "plain"):
+        raise SystemExit("--case takes refined|plain N NM")
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    A, B = gen_batch(n, nm, gen, dev)
+    ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+    del A, B
+    ap, bp = ap0.clone(), bp0.clone()
+    work = torch.empty(max(1, cbk.dposv_refined_lwork(n, NRHS, V, nm)), dtype=torch.uint8,
+                       device=dev)
+    for _ in range(2):
+        ap.copy_(ap0)
+        bp.copy_(bp0)
+        if kind == "refined":
+            info = cbk.dposv_refined_compact("C", "L", n, NRHS, ap, n, bp, n, V, nm, 10, None,
+                                             None, work)
+        else:
+            info = cbk.dposv_compact("C", "L", n, NRHS, ap, n, bp, n, V, nm)
+        assert info == 0, info
+    torch.cuda.synchronize()
+    print("case", kind, n, nm, "ok")
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -747,10 +779,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5"), default="c3",
                     help="c3 (default) is the headline; the others print their own line")
+    ap.add_argument("--case", nargs=3, metavar=("KIND", "N", "NM"),
+                    help="no timing: solve one batch (refined|plain, order N, NM matrices) "
+                         "twice, for a profiler capture")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3  # at least three untimed warm-up steps
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.config != "c3":
         run_config(args)
