@@ -1,6 +1,6 @@
 // cbk_kernels_generic.cu -- the lane-per-matrix kernels for every routine,
 // any order, layout, triangle, side and transpose (the complete drop-in
-// surface). The small-order Cholesky / LDL^T kernels with the matrix held in
+// surface). The small-order Cholesky kernels with the matrix held in
 // registers live in cbk_kernels_chol_reg.cu and take over where they apply.
 #include "cbk_device.cuh"
 #include "cbk_launch.h"
@@ -127,6 +127,8 @@ cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, 
 {
     const long ng = groups_of(nm, V);
     const size_t sa = gstride(row, ldap, n, n, V);
+    if (!ldlt && chol_small_ok(n))
+        return launch_chol_small<T>(false, row, up, n, 0, ap, ldap, nullptr, 1, V, nm, s);
     const int th = threads_for(ldlt ? R_SYTRFNP : R_POTRF, n, sizeof(T));
     if (ldlt)
         k_factor<T, true><<<blocks_for(ng, V, th), th, 0, s>>>(row, up, n, ap, ldap, V, ng, sa);
@@ -230,6 +232,8 @@ template <typename T>
 cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, int nrhs, T *ap,
                              int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s)
 {
+    if (!ldlt && fused && chol_small_ok(n))
+        return launch_chol_small<T>(true, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, s);
     return launch_sym_solve_generic<T>(ldlt, fused, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
                                        s);
 }

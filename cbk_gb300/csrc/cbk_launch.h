@@ -44,6 +44,14 @@ template <typename T>
 cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, int V, int nm,
                           cudaStream_t s);
 
+// Cholesky factor (+ solve when `solve`) of orders 1 .. CHOL_SMALL_NMAX with the
+// matrix in registers (cbk_kernels_chol_reg.cu): the generic kernels' bits
+constexpr int CHOL_SMALL_NMAX = 8;
+bool chol_small_ok(int n);
+template <typename T>
+cudaError_t launch_chol_small(bool solve, bool row, bool up, int n, int nrhs, T *ap, int ldap,
+                              T *bp, int ldbp, int V, int nm, cudaStream_t s);
+
 // potrs / posv (ldlt = false), sytrsnp / sysvnp (ldlt = true); fused = factor first
 template <typename T>
 cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, int nrhs, T *ap,
