@@ -505,6 +505,7 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "binding": "the FP64 pipe, not HBM (see fp64_pipe)",
+                     "fp64_frac": (fp64_flops / (dom_ms * 1e-3) / 1e12) / rate if rate else None,
                      "kernel": f"k_posv_refined_warp<{ndom}> (n={ndom})" if 16 < ndom <= 64
                      else f"k_posv_refined (n={ndom})",
                      "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)"},
