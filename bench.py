@@ -304,9 +304,11 @@ def run_case(args):
 
     import cbk_gb300 as cbk
     kind, n, nm = args.case[0], int(args.case[1]), int(args.case[2])
-    if kind not in ("refined", "plain"):
-        raise SystemExit("--case takes refined|plain N NM")
+    if kind not in ("refined", "plain", "gels_refined", "gels"):
+        raise SystemExit("--case takes refined|plain|gels_refined|gels N NM")
     dev = torch.device("cuda", 0)
+    if kind.startswith("gels"):
+        return run_gels_case(kind, n, nm, dev)
     gen = torch.Generator(device=dev)
     gen.manual_seed(SEED)
     A, B = gen_batch(n, nm, gen, dev)
@@ -323,6 +325,57 @@ def run_case(args):
                                              None, work)
         else:
             info = cbk.dposv_compact("C", "L", n, NRHS, ap, n, bp, n, V, nm)
+        assert info == 0, info
+    torch.cuda.synchronize()
+    print("case", kind, n, nm, "ok")
+
+
+def ls_batch(m, n, nrhs, nm, dev):
+    """The least-squares batch: A = U diag(s) V^T with kappa in 1e1 .. 1e4,
+    B = A X + 1e-3 N(0,1), packed at width V on the device; also A and B
+    unpacked (device) for the error checks."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(SEED)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases as C
+    from oracle import oracle as O
+    A, Bm, _, _ = C.gen_ls_cond(rng, nm, m, n, nrhs)
+    ap0 = torch.from_numpy(O.pack(A, V)).to(dev)
+    bp0 = torch.from_numpy(O.pack(Bm, V, pad_diag=0.0)).to(dev)
+    return ap0, bp0, torch.from_numpy(A).to(dev), torch.from_numpy(Bm).to(dev)
+
+
+def ls_normal_residual(A, bp, B, m, n, nrhs, nm):
+    """max over matrices and right-hand sides of ||A^T (b - A x)||_inf /
+    (||A||_inf (||A||_inf ||x||_inf + ||b||_inf)), x read from the packed B."""
+    X = bp.view(nm // V, nrhs, m, V).permute(0, 3, 2, 1).reshape(nm, m, nrhs)[:, :n]
+    G = A.transpose(1, 2) @ (B - A @ X)
+    an = A.abs().sum(dim=2).amax(dim=1)[:, None]
+    den = an * (an * X.abs().amax(dim=1) + B.abs().amax(dim=1))
+    return float((G.abs().amax(dim=1) / den).amax())
+
+
+def run_gels_case(kind, n, nm, dev):
+    """--case gels_refined|gels N NM: the least-squares configuration's shape
+    (m = 4 N, nrhs = 8) on NM matrices, solved twice."""
+    import torch
+
+    import cbk_gb300 as cbk
+    m, nrhs = 4 * n, 8
+    ap0, bp0, _, _ = ls_batch(m, n, nrhs, nm, dev)
+    ap, bp = ap0.clone(), bp0.clone()
+    tau = torch.empty(nm * n, dtype=torch.float64, device=dev)
+    work = torch.empty(max(1, cbk.dgels_refined_lwork(m, n, nrhs, V, nm)), dtype=torch.uint8,
+                       device=dev)
+    for _ in range(2):
+        ap.copy_(ap0)
+        bp.copy_(bp0)
+        if kind == "gels_refined":
+            info = cbk.dgels_refined_compact("C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm, 10,
+                                             None, None, work)
+        else:
+            info = cbk.dgels_compact("C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm)
         assert info == 0, info
     torch.cuda.synchronize()
     print("case", kind, n, nm, "ok")
@@ -732,13 +785,7 @@ def run_config(args):
                                       "45 buckets, V=32: one persistent CUDA-graph launch")
     elif args.config == "c5":
         m, n, nrhs, nm = 64, 16, 8, 131072
-        rng = np.random.default_rng(SEED)
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        import cases as C
-        A, Bm, _, kappa = C.gen_ls_cond(rng, nm, m, n, nrhs)
-        from oracle import oracle as O
-        ap0 = torch.from_numpy(O.pack(A, V)).to(dev)
-        bp0 = torch.from_numpy(O.pack(Bm, V, pad_diag=0.0)).to(dev)
+        ap0, bp0, Ad, Bd = ls_batch(m, n, nrhs, nm, dev)
         ap, bp = ap0.clone(), bp0.clone()
         tau = torch.empty(nm * n, dtype=f64, device=dev)
         it = torch.empty(nm, dtype=torch.int32, device=dev)
@@ -752,15 +799,19 @@ def run_config(args):
             "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm, 10, it, None, work)) or 1, restore,
             args.steps, args.warmup)
         itc = it.cpu().numpy()
+        ne_ref = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
         tpl, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact("C", "N", m, n, nrhs, ap, m,
                                                                    bp, m, tau, V, nm)) or 1,
                        restore, args.steps, args.warmup)
+        ne_pl = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
         line.update(metric="least squares 64x16 nrhs=8 solves/s: refined FP32 vs plain FP64",
                     value=nm / (tr * 1e-3), unit=UNIT, ms_per_step=tr,
                     dtype="f32 QR + f64 refinement", data="synthetic: A = U diag(s) V^T, kappa "
                     "1e1..1e4, B = A X + 1e-3 N(0,1)",
                     plain_fp64={"value": nm / (tpl * 1e-3), "ms_per_step": tpl},
                     speedup_refined_vs_plain=tpl / tr,
+                    max_normal_residual_over_n_eps={"refined": ne_ref / (n * 2.220446049250313e-16),
+                                                    "plain": ne_pl / (n * 2.220446049250313e-16)},
                     refinement={"converged_frac": float((itc >= 0).mean()),
                                 "mean_steps": float(itc[itc >= 0].mean())},
                     gpu_launches=args.steps)

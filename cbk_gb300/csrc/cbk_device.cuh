@@ -142,6 +142,19 @@ __device__ __forceinline__ bool beyond_fp32(double a)
     return big && !nan;
 }
 
+// 8-byte asynchronous copy global -> shared (cp.async, cached in L1 and L2)
+__device__ __forceinline__ void cp_async8(double *dst, const double *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+// wait for every cp.async this thread issued
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // max(a, b) that keeps a NaN (fmaxf drops it): a NaN residual norm must stop
 // a refinement rather than pass its convergence test
 __device__ __forceinline__ float fmax_nan(float a, float b)
@@ -613,6 +626,21 @@ __device__ void gels_lane(bool overdet, int p, int q, int nrhs, LV<T> F, T *tau,
         trsm_lane<T>(true, true, true, false, q, nrhs, T(1), F, B);
         zero_lane<T>(B, q, p, nrhs);
         ormqr_lane<T>(false, p, nrhs, q, F, tau, V, B);
+    }
+}
+
+// The plain FP64 least squares of one lane, the fallback of the
+// mixed-precision solves: QR of A in place (tau), then the right-hand sides
+// first .. nrhs-1 of B solved through Q^T and R.
+__device__ __forceinline__ void gels_fallback_lane(int m, int n, int nrhs, int first, LV<double> A,
+                                                   double *taup, int V, LV<double> B)
+{
+    geqrf_lane<double>(m, n, A, taup, V);
+    if (first < nrhs) {
+        LV<double> Bs = B;
+        Bs.p += (long)first * B.sj;
+        ormqr_lane<double>(true, m, nrhs - first, n, A, taup, V, Bs);
+        trsm_lane<double>(true, true, false, false, n, nrhs - first, 1.0, A, Bs);
     }
 }
 

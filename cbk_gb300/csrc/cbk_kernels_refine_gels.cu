@@ -50,18 +50,6 @@ struct GelsWork {
     double *r;  // m per lane: the FP64 residual estimate
 };
 
-__device__ __forceinline__ void gels_fallback(int m, int n, int nrhs, int first, LV<double> A,
-                                           double *taup, int V, LV<double> B)
-{
-    geqrf_lane<double>(m, n, A, taup, V);
-    if (first < nrhs) {
-        LV<double> Bs = B;
-        Bs.p += (long)first * B.sj;
-        ormqr_lane<double>(true, m, nrhs - first, n, A, taup, V, Bs);
-        trsm_lane<double>(true, true, false, false, n, nrhs - first, 1.0, A, Bs);
-    }
-}
-
 __global__ void __launch_bounds__(128, 4)
     k_gels_refined(bool row, int m, int n, int nrhs, double *ap, int ldap, double *bp, int ldbp,
                    double *taup, int V, long ngroups, size_t sa, size_t sb, GelsWork w,
@@ -199,7 +187,7 @@ __global__ void __launch_bounds__(128, 4)
         }
     }
     if (status != 0)
-        gels_fallback(m, n, nrhs, status == -3 ? col - 1 : 0, A, tau64, V, B);
+        gels_fallback_lane(m, n, nrhs, status == -3 ? col - 1 : 0, A, tau64, V, B);
     if (idx < nm) {
         if (iters) iters[idx] = status != 0 ? status : it_max;
         if (berr) berr[idx] = status != 0 ? (double)NAN : (double)worst;
@@ -232,6 +220,10 @@ cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, in
                                 int ldbp, double *taup, int V, int nm, int max_iter, int *iters,
                                 double *berr, void *work, cudaStream_t s)
 {
+    // variant 0: one warp per matrix where it is compiled; 1: one lane per matrix
+    if (gels_refined_warp_ok(m, n) && variant_for(R_GELS_REFINED, n, 8) == 0)
+        return launch_gels_refined_warp(row, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
+                                        max_iter, iters, berr, s);
     const long ng = ((long)nm + V - 1) / V;
     const size_t lanes = (size_t)ng * V;
     char *base = static_cast<char *>(work);

@@ -80,19 +80,6 @@ __device__ __forceinline__ float exp2i(int k)
     return __int_as_float((127 + k) << 23);
 }
 
-// 8-byte asynchronous copy global -> shared (cp.async, cached in L1 and L2)
-__device__ __forceinline__ void cp_async8(double *dst, const double *src)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-
-// wait for every cp.async this thread issued
-__device__ __forceinline__ void cp_async_wait_all()
-{
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
-
 __device__ __forceinline__ float warp_max(float v)
 {
 #pragma unroll

@@ -94,6 +94,11 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
 // mixed-precision least squares (cbk_kernels_refine_gels.cu)
 size_t gels_refined_lwork(int m, int n, int nrhs, int V, int nm);
 int gels_refined_nmax();
+// the warp-per-matrix refined least squares (m <= 64, n in {8, 16})
+bool gels_refined_warp_ok(int m, int n);
+cudaError_t launch_gels_refined_warp(bool row, int m, int n, int nrhs, double *ap, int ldap,
+                                     double *bp, int ldbp, double *taup, int V, int nm,
+                                     int max_iter, int *iters, double *berr, cudaStream_t s);
 cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, int ldap, double *bp,
                                 int ldbp, double *taup, int V, int nm, int max_iter, int *iters,
                                 double *berr, void *work, cudaStream_t s);

@@ -4,7 +4,8 @@
 // lane-per-matrix kernel for a routine at order n and scalar size dsize;
 // variant_for(...) picks between a kernel's compiled shapes where it has more
 // than one (for the warp-per-matrix refined solve: registers per thread
-// against resident blocks); vlen_for(...) is the interleave width the
+// against resident blocks; for the refined least squares: 0 one warp per
+// matrix where compiled, 1 one lane per matrix); vlen_for(...) is the interleave width the
 // autotuner measured fastest (advice for the caller's layout: the width of a
 // batch is the caller's). All default to 0 (the built-in choice); the
 // autotuner (cbk_cuda_autotune, cbk_autotune.cu) overwrites entries with
@@ -132,6 +133,7 @@ constexpr Name NAMES[] = {
     {"posv", R_POSV},     {"sytrsnp", R_SYTRSNP}, {"sysvnp", R_SYSVNP},
     {"trsm", R_TRSM},     {"geqrf", R_GEQRF},     {"ormqr", R_ORMQR},
     {"orgqr", R_ORGQR},   {"gels", R_GELS},       {"posv_refined", R_POSV_REFINED},
+    {"gels_refined", R_GELS_REFINED},
 };
 
 } // namespace

@@ -397,8 +397,11 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
  * (advice for the caller's packing; a batch's width is the caller's). Entry
  * 0 means the built-in choice. Launch shapes never change results.
  * routine: "potrf", "sytrfnp", "potrs", "posv", "sytrsnp", "sysvnp", "trsm",
- * "geqrf", "ormqr", "orgqr", "gels" or "posv_refined"; prec 'd' or 's' ('d'
- * only for posv_refined); the order is n, except m for the QR routines.
+ * "geqrf", "ormqr", "orgqr", "gels", "posv_refined" or "gels_refined"; prec
+ * 'd' or 's' ('d' only for the refined solves); the order is n, except m for
+ * the QR routines. "gels_refined" has one entry, set by cbk_cuda_tune_set
+ * (not autotuned): variant 0 runs one warp per matrix where that kernel is
+ * compiled (m <= 64, n = 8 or 16), variant 1 one lane per matrix.
  *
  * cbk_cuda_autotune times the routine on a synthetic batch of nm matrices
  * (m x n for the QR routines, m >= n; n x n otherwise; nrhs right-hand

@@ -27,8 +27,23 @@ def _normal_residual(A, X, B):
     return (np.abs(G).max(axis=1) / (an[:, None] * (an[:, None] * xn + bn))).max(axis=1)
 
 
-@pytest.mark.parametrize("m,n,nrhs", [(64, 16, 8), (20, 6, 1), (33, 17, 3), (16, 16, 2)])
-def test_refined_gels_meets_fp64_accuracy(m, n, nrhs, cuda):
+# (64, 16, 8), (16, 16, 2), (40, 8, 4) and (12, 8, 3) run the warp-per-matrix
+# kernel (variant 0); lane=True forces the lane-per-matrix one
+@pytest.mark.parametrize("m,n,nrhs,lane", [(64, 16, 8, False), (20, 6, 1, False),
+                                           (33, 17, 3, False), (16, 16, 2, False),
+                                           (40, 8, 4, False), (12, 8, 3, False),
+                                           (64, 16, 8, True), (40, 8, 4, True)])
+def test_refined_gels_meets_fp64_accuracy(m, n, nrhs, lane, cuda):
+    import cbk_gb300
+    if lane:
+        assert cbk_gb300.tune_set("gels_refined", "d", n, variant=1) == 0
+    try:
+        _check_refined_gels(m, n, nrhs)
+    finally:
+        cbk_gb300.tune_reset()
+
+
+def _check_refined_gels(m, n, nrhs):
     import torch
 
     import cbk_gb300
@@ -81,3 +96,52 @@ def test_refined_gels_argument_checks(cuda):
     assert f("C", "N", 80, 70, 1, None, 80, None, 80, None, 32, 64) == -4
     assert f("C", "N", 8, 4, 1, None, 8, None, 8, None, 32, 64, max_iter=-1) == -13
     assert f("C", "N", 8, 4, 0, None, 8, None, 8, None, 32, 64) == 0
+
+
+@pytest.mark.parametrize("m,n,nrhs,lane", [(64, 16, 3, False), (40, 8, 2, False),
+                                           (64, 16, 3, True), (20, 6, 2, False)])
+def test_refined_gels_fallback_is_the_plain_solve(m, n, nrhs, lane, cuda):
+    """Matrices beyond the FP32 range (iters -2) and with a NaN (-3) are solved
+    by the plain FP64 path: A, tau and B bit-identical to dgels_compact's; the
+    other matrices converge and leave A and tau untouched."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(7 * m + n)
+    nm, V = 96, 32
+    A, B, _, _ = C.gen_ls_cond(rng, nm, m, n, nrhs)
+    big, nan = [3, 40, 95], [10, 64]
+    A[big] *= 1e42
+    A[nan, 1, 0] = np.nan
+    ap, bp = O.pack(A, V), O.pack(B, V, pad_diag=0.0)
+    ng = (nm + V - 1) // V
+    if lane:
+        assert cbk_gb300.tune_set("gels_refined", "d", n, variant=1) == 0
+    try:
+        a1, b1 = torch.from_numpy(ap).cuda(), torch.from_numpy(bp).cuda()
+        t1 = torch.zeros(ng * V * n, dtype=torch.float64, device="cuda")
+        it = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+        be = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+        assert cbk_gb300.dgels_refined_compact("C", "N", m, n, nrhs, a1, m, b1, m, t1, V, nm,
+                                               iters=it, berr=be) == 0
+        a2, b2 = torch.from_numpy(ap).cuda(), torch.from_numpy(bp).cuda()
+        t2 = torch.zeros(ng * V * n, dtype=torch.float64, device="cuda")
+        assert cbk_gb300.dgels_compact("C", "N", m, n, nrhs, a2, m, b2, m, t2, V, nm) == 0
+        torch.cuda.synchronize()
+    finally:
+        cbk_gb300.tune_reset()
+    it, be = it.cpu().numpy(), be.cpu().numpy()
+    assert (it[big] == -2).all() and (it[nan] == -3).all()
+    ok = np.setdiff1d(np.arange(nm), big + nan)
+    assert (it[ok] >= 0).all()
+    assert np.isnan(be[big + nan]).all() and (be[ok] <= 8 * n * EPS).all()
+    A1, A2 = O.unpack(a1.cpu().numpy(), nm, m, n, V), O.unpack(a2.cpu().numpy(), nm, m, n, V)
+    B1, B2 = (O.unpack(x.cpu().numpy(), nm, m, nrhs, V) for x in (b1, b2))
+    T1 = t1.cpu().numpy().reshape(ng, n, V).transpose(0, 2, 1).reshape(-1, n)[:nm]
+    T2 = t2.cpu().numpy().reshape(ng, n, V).transpose(0, 2, 1).reshape(-1, n)[:nm]
+    fb = big + nan
+    assert np.array_equal(A1[fb], A2[fb], equal_nan=True)
+    assert np.array_equal(B1[fb], B2[fb], equal_nan=True)
+    assert np.array_equal(T1[fb], T2[fb], equal_nan=True)
+    assert np.array_equal(A1[ok], O.unpack(ap, nm, m, n, V)[ok])
+    assert (T1[ok] == 0).all()
