@@ -80,6 +80,52 @@ __device__ __forceinline__ float exp2i(int k)
     return __int_as_float((127 + k) << 23);
 }
 
+// Two FP32 values in one 64-bit register pair, for sm_100's packed FP32 FMA
+// (fma.rn.f32x2: two IEEE fmaf in one instruction, bit-identical to them).
+// The FP32 rows live in such pairs, so the sweep and the matrix-vector
+// products issue half the FMA instructions.
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2(float lo, float hi)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ float f2lo(f2_t p)
+{
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p));
+    return a;
+}
+
+__device__ __forceinline__ float f2hi(f2_t p)
+{
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p));
+    return b;
+}
+
+// d = a * b + c, element-wise
+__device__ __forceinline__ f2_t ffma2(f2_t a, f2_t b, f2_t c)
+{
+    f2_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// element q (static) of a row held in pairs
+template <int P> __device__ __forceinline__ float el(const f2_t (&R)[P], int q)
+{
+    return (q & 1) ? f2hi(R[q >> 1]) : f2lo(R[q >> 1]);
+}
+
+template <int P> __device__ __forceinline__ void set_el(f2_t (&R)[P], int q, float v)
+{
+    R[q >> 1] = (q & 1) ? f2(f2lo(R[q >> 1]), v) : f2(v, f2hi(R[q >> 1]));
+}
+
 __device__ __forceinline__ float warp_max(float v)
 {
 #pragma unroll
@@ -139,6 +185,8 @@ template <int N> struct Rows {
     static constexpr bool SPLIT = TWO && N <= 48;
     static constexpr int H = N / 2;
     static constexpr int W1 = !TWO ? 1 : (SPLIT ? H : N);
+    static constexpr int P0 = N / 2;          // pairs of R0
+    static constexpr int P1 = (W1 + 1) / 2;   // pairs of R1
 };
 
 // z := -M z for this lane's rows, with M = -(D A D)^-1 in R0 / R1 and z
@@ -146,8 +194,8 @@ template <int N> struct Rows {
 // D z is then A32^-1 v. Row lane + 32 r is z[r] (lanes 0..15 for r = 1 when
 // the second rows are split). Two partial sums per row break the FMA chain.
 template <int N>
-__device__ __forceinline__ void apply_inverse(int lane, const float (&R0)[N],
-                                              const float (&R1)[Rows<N>::W1], float *SR,
+__device__ __forceinline__ void apply_inverse(int lane, const f2_t (&R0)[Rows<N>::P0],
+                                              const f2_t (&R1)[Rows<N>::P1], float *SR,
                                               float (&z)[(N + 31) / 32])
 {
     using L = Rows<N>;
@@ -157,30 +205,32 @@ __device__ __forceinline__ void apply_inverse(int lane, const float (&R0)[N],
     for (int r = 0; r < NR; ++r)
         if (lane + 32 * r < N) SR[lane + 32 * r] = z[r];
     __syncwarp();
-    float a0[2] = {0.f, 0.f}, a1[2] = {0.f, 0.f};
+    // the even and odd columns' partial sums are the two halves of a pair
+    const f2_t *SP = reinterpret_cast<const f2_t *>(SR);
+    f2_t a0 = 0ull, a1 = 0ull;
     if constexpr (L::SPLIT) {
         const bool lower = lane < 16;
 #pragma unroll
-        for (int t = 0; t < L::H; ++t) {
-            const float za = SR[t], zb = SR[t + L::H];
-            a0[t & 1] = fmaf(R0[t], za, a0[t & 1]);
-            a0[t & 1] = fmaf(R0[t + L::H], zb, a0[t & 1]);
-            a1[t & 1] = fmaf(R1[t], lower ? za : zb, a1[t & 1]);
+        for (int t = 0; t < L::H / 2; ++t) {
+            const f2_t za = SP[t], zb = SP[t + L::H / 2];
+            a0 = ffma2(R0[t], za, a0);
+            a0 = ffma2(R0[t + L::H / 2], zb, a0);
+            a1 = ffma2(R1[t], lower ? za : zb, a1);
         }
-        float b = a1[0] + a1[1];
+        float b = f2lo(a1) + f2hi(a1);
         b += __shfl_xor_sync(FULL, b, 16);
-        z[0] = -(a0[0] + a0[1]);
+        z[0] = -(f2lo(a0) + f2hi(a0));
         z[1] = -b;
     }
     else {
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-            const float zj = SR[j];
-            a0[j & 1] = fmaf(R0[j], zj, a0[j & 1]);
-            if constexpr (L::TWO) a1[j & 1] = fmaf(R1[j], zj, a1[j & 1]);
+        for (int j = 0; j < N / 2; ++j) {
+            const f2_t zj = SP[j];
+            a0 = ffma2(R0[j], zj, a0);
+            if constexpr (L::TWO) a1 = ffma2(R1[j], zj, a1);
         }
-        z[0] = -(a0[0] + a0[1]);
-        if constexpr (L::TWO) z[NR - 1] = -(a1[0] + a1[1]);
+        z[0] = -(f2lo(a0) + f2hi(a0));
+        if constexpr (L::TWO) z[NR - 1] = -(f2lo(a1) + f2hi(a1));
     }
 }
 
@@ -347,7 +397,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     __syncwarp();
     using L = Rows<N>;
     constexpr int H = L::H;
-    float R0[N], R1[L::W1];
+    f2_t R0[L::P0], R1[L::P1]; // the FP32 rows, in pairs of columns
     unsigned hmax = 0; // largest high word of |a| read: a quick screen for the FP32 range
     float rs = 0.f;
     {
@@ -355,19 +405,23 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         const int ci = pk_col(N, i) - i;
         const bool real = N >= 32 || lane < N;
         const float di = exp2i(-h[0]);
-        float sum = 0.f;
+        float sum = 0.f, prev = 0.f;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
             const double a = SA[j <= i ? pk_col(N, j) - j + i : ci + j];
             hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
             const float f = d2f_rz_inrange(a);
             sum += fabsf(f);
-            R0[j] = real ? f * (di * SR[j]) : 0.f;
+            const float e = real ? f * (di * SR[j]) : 0.f;
+            if (j & 1)
+                R0[j >> 1] = f2(prev, e);
+            else
+                prev = e;
         }
         if (lane < n) rs = sum;
     }
     if constexpr (!L::TWO) {
-        R1[0] = 0.f;
+        R1[0] = 0ull;
     }
     else if constexpr (L::SPLIT) {
         const bool lower = lane < 16;
@@ -376,7 +430,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         const int ci = pk_col(N, i) - i;
         const bool real = N >= 48 || ib < N;
         const float di = SR[i];
-        float sum = 0.f;
+        float sum = 0.f, prev = 0.f;
 #pragma unroll
         for (int t = 0; t < H; ++t) {
             const int j = (lower ? 0 : H) + t;
@@ -386,7 +440,11 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
             hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
             const float f = d2f_rz_inrange(a);
             sum += fabsf(f);
-            R1[t] = real ? f * (di * SR[j]) : 0.f;
+            const float e = real ? f * (di * SR[j]) : 0.f;
+            if (t & 1)
+                R1[t >> 1] = f2(prev, e);
+            else
+                prev = e;
         }
         sum += __shfl_xor_sync(FULL, sum, 16);
         if (ib < n) rs = fmaxf(rs, sum);
@@ -396,14 +454,18 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         const int ci = pk_col(N, i) - i;
         const bool real = lane + 32 < N;
         const float di = exp2i(-h[1]);
-        float sum = 0.f;
+        float sum = 0.f, prev = 0.f;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
             const double a = SA[j <= i ? pk_col(N, j) - j + i : ci + j];
             hmax = max(hmax, (unsigned)__double2hiint(a) & 0x7fffffffu);
             const float f = d2f_rz_inrange(a);
             sum += fabsf(f);
-            R1[j] = real ? f * (di * SR[j]) : 0.f;
+            const float e = real ? f * (di * SR[j]) : 0.f;
+            if (j & 1)
+                R1[j >> 1] = f2(prev, e);
+            else
+                prev = e;
         }
         if (lane + 32 < n) rs = fmaxf(rs, sum);
     }
@@ -440,19 +502,22 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         for (int u = 0; u < U; ++u) {
             const int k = k0 + u;
             float *const S = (u & 1) ? SC + 2 * N : SC;
-            // c[q] = column (k0 + q) mod N from the doubled column; the upper
-            // half of a split row reads from c[H] on
-            const float4 *C4 = reinterpret_cast<const float4 *>(S + k0);
-            const float4 *CB4 =
-                reinterpret_cast<const float4 *>(S + k0 + ((L::SPLIT && lane >= 16) ? H : 0));
+            // c = column (k0 + q) mod N from the doubled column, read in
+            // pairs; the upper half of a split row reads from c[H] on
+            const ulonglong2 *C4 = reinterpret_cast<const ulonglong2 *>(S + k0);
+            const ulonglong2 *CB4 =
+                reinterpret_cast<const ulonglong2 *>(S + k0 + ((L::SPLIT && lane >= 16) ? H : 0));
+            const float r0u = el(R0, u);
             if (N >= 32 || lane < N) {
-                S[lane] = R0[u];
-                S[lane + N] = R0[u];
+                S[lane] = r0u;
+                S[lane + N] = r0u;
             }
+            float r1u = 0.f;
             if constexpr (L::TWO) {
+                r1u = el(R1, u);
                 if ((!L::SPLIT || lane < 16) && 32 + lane < N) {
-                    S[32 + lane] = R1[u];
-                    S[32 + lane + N] = R1[u];
+                    S[32 + lane] = r1u;
+                    S[32 + lane + N] = r1u;
                 }
             }
             __syncwarp();
@@ -460,89 +525,105 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
             nonpos |= !(p > 0.f);
             const float rp = rcp_approx(p);
             const bool own0 = lane == k;
-            const float w0 = R0[u] * rp;
+            const float w0 = r0u * rp;
             const float beta0 = own0 ? rp - 1.0f : -w0;
             const float last0 = own0 ? -rp : w0;
             float betab = 0.f, lastb = 0.f;
             if constexpr (L::TWO) {
-                float vb = R1[u];
+                float vb = r1u;
                 if constexpr (L::SPLIT) {
-                    const float o = __shfl_xor_sync(FULL, R1[u], 16);
-                    vb = lane < 16 ? R1[u] : o; // column k of row 32 + lane % 16
+                    const float o = __shfl_xor_sync(FULL, r1u, 16);
+                    vb = lane < 16 ? r1u : o; // column k of row 32 + lane % 16
                 }
                 const bool ownb = (L::SPLIT ? 32 + (lane & 15) : 32 + lane) == k;
                 const float wb = vb * rp;
                 betab = ownb ? rp - 1.0f : -wb;
                 lastb = ownb ? -rp : wb;
             }
+            const f2_t bb0 = f2(beta0, beta0), bb1 = f2(betab, betab);
+            const int PU = u >> 1, UO = u ^ 1; // u's pair, the other column in it
 #pragma unroll
             for (int q4 = 0; q4 < N / 4; ++q4) {
-                const float4 c4 = C4[q4];
-                const float cq[4] = {c4.x, c4.y, c4.z, c4.w};
+                const ulonglong2 c = C4[q4];
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int q = 4 * q4 + e;
-                    if (q != u) {
-                        R0[q] = fmaf(beta0, cq[e], R0[q]);
-                        if constexpr (L::TWO && !L::SPLIT) R1[q] = fmaf(betab, cq[e], R1[q]);
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int P = 2 * q4 + hh;
+                    const f2_t cp = hh ? c.y : c.x;
+                    if (P != PU) {
+                        R0[P] = ffma2(bb0, cp, R0[P]);
+                        if constexpr (L::TWO && !L::SPLIT) R1[P] = ffma2(bb1, cp, R1[P]);
+                    }
+                    else {
+                        // column u takes its final value; the other is updated
+                        const float co = (UO & 1) ? f2hi(cp) : f2lo(cp);
+                        const float n0 = fmaf(beta0, co, el(R0, UO));
+                        R0[P] = (u & 1) ? f2(n0, last0) : f2(last0, n0);
+                        if constexpr (L::TWO && !L::SPLIT) {
+                            const float n1 = fmaf(betab, co, el(R1, UO));
+                            R1[P] = (u & 1) ? f2(n1, lastb) : f2(lastb, n1);
+                        }
                     }
                 }
             }
-            R0[u] = last0;
-            if constexpr (L::TWO && !L::SPLIT) R1[u] = lastb;
             if constexpr (L::SPLIT) {
 #pragma unroll
                 for (int t4 = 0; t4 < H / 4; ++t4) {
-                    const float4 c4 = CB4[t4];
-                    const float cq[4] = {c4.x, c4.y, c4.z, c4.w};
+                    const ulonglong2 c = CB4[t4];
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int t = 4 * t4 + e;
-                        const float nv = fmaf(betab, cq[e], R1[t]);
-                        // the pivot column sits in the lower half (u < 8 <= H)
-                        R1[t] = (t == u && lane < 16) ? lastb : nv;
+                    for (int hh = 0; hh < 2; ++hh) {
+                        const int P = 2 * t4 + hh;
+                        const f2_t nv = ffma2(bb1, hh ? c.y : c.x, R1[P]);
+                        if (P == PU) {
+                            // the pivot column sits in the lower half (u < 8 <= H)
+                            const float eu = lane < 16 ? lastb : ((u & 1) ? f2hi(nv) : f2lo(nv));
+                            R1[P] = (u & 1) ? f2(f2lo(nv), eu) : f2(eu, f2hi(nv));
+                        }
+                        else {
+                            R1[P] = nv;
+                        }
                     }
                 }
             }
         }
-        // rotate by U: register q takes column k0 + U + q
+        // rotate by U: register pair q takes columns k0 + U + 2q, +1
+        constexpr int UP = U / 2;
         {
-            float t0[U];
+            f2_t t0[UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
+            for (int e = 0; e < UP; ++e)
                 t0[e] = R0[e];
 #pragma unroll
-            for (int q = 0; q < N - U; ++q)
-                R0[q] = R0[q + U];
+            for (int q = 0; q < L::P0 - UP; ++q)
+                R0[q] = R0[q + UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
-                R0[N - U + e] = t0[e];
+            for (int e = 0; e < UP; ++e)
+                R0[L::P0 - UP + e] = t0[e];
         }
         if constexpr (L::TWO && !L::SPLIT) {
-            float t1[U];
+            f2_t t1[UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
+            for (int e = 0; e < UP; ++e)
                 t1[e] = R1[e];
 #pragma unroll
-            for (int q = 0; q < N - U; ++q)
-                R1[q] = R1[q + U];
+            for (int q = 0; q < L::P1 - UP; ++q)
+                R1[q] = R1[q + UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
-                R1[N - U + e] = t1[e];
+            for (int e = 0; e < UP; ++e)
+                R1[L::P1 - UP + e] = t1[e];
         }
         if constexpr (L::SPLIT) {
             // lower half: V[t] = V[t + 8], the last 8 from the upper half's
             // first 8; upper half: the same, the last 8 from the lower half's
-            float t1[U];
+            f2_t t1[UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
+            for (int e = 0; e < UP; ++e)
                 t1[e] = __shfl_xor_sync(FULL, R1[e], 16);
 #pragma unroll
-            for (int t = 0; t < H - U; ++t)
-                R1[t] = R1[t + U];
+            for (int q = 0; q < L::P1 - UP; ++q)
+                R1[q] = R1[q + UP];
 #pragma unroll
-            for (int e = 0; e < U; ++e)
-                R1[H - U + e] = t1[e];
+            for (int e = 0; e < UP; ++e)
+                R1[L::P1 - UP + e] = t1[e];
         }
     }
     if (nonpos && status == 0) status = -1;
