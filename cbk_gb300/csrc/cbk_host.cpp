@@ -27,8 +27,14 @@ namespace cbkcuda {
 namespace {
 
 constexpr int NBUF = 3;
-constexpr long CHUNKS = 16;         // chunks per batch, unless that makes them small
+// A chunk moves about CHUNK_BYTES over the link (A's triangle and B), so its
+// copy outlasts the host's few calls per chunk; it holds at least
+// MIN_CHUNK_GROUPS groups, so its solve fills the GPU. The first and the
+// last chunk are a quarter of that (at least MIN_RAMP_GROUPS): the first
+// solve starts after a short copy, and the last copy leaves a short solve.
+constexpr size_t CHUNK_BYTES = (size_t)48 << 20;
 constexpr long MIN_CHUNK_GROUPS = 256;
+constexpr long MIN_RAMP_GROUPS = 64;
 
 inline size_t align256(size_t b)
 {
@@ -36,18 +42,32 @@ inline size_t align256(size_t b)
 }
 
 struct Plan {
-    long ngroups, chunk;   // groups in the batch and per chunk
-    size_t ga, gb;         // bytes of one group of A and of B
+    long ngroups, chunk, ramp; // groups in the batch, per chunk (a slot), in the first and last
+    size_t ga, gb;             // bytes of one group of A and of B
     size_t a, b, it, be, cnt, ws, slot; // bytes of each part of one slot
+
+    // the size of the chunk that starts at group g0: the first is `ramp`,
+    // then `chunk` while more than chunk + ramp remain, then the rest but
+    // `ramp`, then `ramp`
+    long at(long g0) const
+    {
+        const long left = ngroups - g0;
+        if (g0 == 0 || left <= ramp) return std::min(left, ramp);
+        if (left > chunk + ramp) return chunk;
+        return left - ramp;
+    }
 };
 
 Plan plan(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm)
 {
     Plan p{};
     p.ngroups = ((long)nm + V - 1) / V;
-    p.chunk = std::min(p.ngroups, std::max(MIN_CHUNK_GROUPS, (p.ngroups + CHUNKS - 1) / CHUNKS));
     p.ga = (size_t)ldap * n * V * sizeof(double);
     p.gb = (size_t)ldbp * (row ? n : nrhs) * V * sizeof(double);
+    const size_t moved = (size_t)n * (n + 1) / 2 * V * sizeof(double) + p.gb;
+    const long want = (long)((CHUNK_BYTES + moved - 1) / moved);
+    p.chunk = std::min(p.ngroups, std::max(MIN_CHUNK_GROUPS, want));
+    p.ramp = std::min(p.chunk, std::max(MIN_RAMP_GROUPS, p.chunk / 4));
     const size_t lanes = (size_t)p.chunk * V;
     p.a = align256(p.chunk * p.ga);
     p.b = align256(p.chunk * p.gb);
@@ -148,11 +168,12 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         sl.g0 = -1;
     };
 
-    for (long g0 = 0, c = 0; g0 < p.ngroups && err == cudaSuccess; g0 += p.chunk, ++c) {
+    for (long g0 = 0, c = 0, groups = 0; g0 < p.ngroups && err == cudaSuccess;
+         g0 += groups, ++c) {
         Slot &sl = slot[c % NBUF];
         finish(sl);
         if (err != cudaSuccess) break;
-        const long groups = std::min(p.chunk, p.ngroups - g0);
+        groups = p.at(g0);
         const long lane0 = g0 * V;
         const int nmc = (int)std::min((long)nm - lane0, groups * V);
         // the slot is idle (finish), so its inputs may be overwritten now

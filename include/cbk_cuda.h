@@ -254,9 +254,11 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
  * pointers; pinned memory lets the copies overlap the solves). No reference
  * entry point: the reference's own calling convention -- every array on the
  * host, as in ?posv_compact (include/cbk.h:218-234) -- over the device solve
- * above. The batch is cut into chunks of whole groups that pass through
- * three device slots on three streams, so that copying one chunk in, solving
- * another and copying a third out overlap. When ap is pinned (or registered)
+ * above. The batch is cut into chunks of whole groups (about 48 MiB of
+ * input each, at least 256 groups; the first and last a quarter of that)
+ * that pass through three device slots on three streams, so that copying one
+ * chunk in, solving another and copying a third out overlap. The workspace
+ * is therefore bounded whatever nm. When ap is pinned (or registered)
  * host memory, the device reads only the referenced triangle of A from it
  * directly; otherwise each chunk's A moves as one contiguous copy. B moves as
  * one contiguous copy each way. B (X) is copied back; A is copied back only for a
