@@ -95,15 +95,15 @@ __device__ __forceinline__ f2_t f2(float lo, float hi)
 
 __device__ __forceinline__ float f2lo(f2_t p)
 {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p));
+    float a;
+    asm("{\n\t.reg .f32 t;\n\tmov.b64 {%0, t}, %1;\n\t}" : "=f"(a) : "l"(p));
     return a;
 }
 
 __device__ __forceinline__ float f2hi(f2_t p)
 {
-    float a, b;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p));
+    float b;
+    asm("{\n\t.reg .f32 t;\n\tmov.b64 {t, %0}, %1;\n\t}" : "=f"(b) : "l"(p));
     return b;
 }
 
