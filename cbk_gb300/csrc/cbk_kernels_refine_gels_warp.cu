@@ -530,10 +530,13 @@ cudaError_t launch_warp_gels(bool row, int m, int nrhs, double *ap, int ldap, do
 {
     constexpr int WPB = 4;
     const size_t smem = (size_t)WPB * GW<MR, N>::BYTES;
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_gels_refined_warp<MR, N, WPB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)smem);
-    if (attr != cudaSuccess) return attr;
+    // per device, so on every launch (the current device may change)
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gels_refined_warp<MR, N, WPB, MINB>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     const long ng = ((long)nm + V - 1) / V;
     const long total = ng * V;
     const unsigned blocks = (unsigned)((total + WPB - 1) / WPB);
