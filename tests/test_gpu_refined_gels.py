@@ -145,3 +145,34 @@ def test_refined_gels_fallback_is_the_plain_solve(m, n, nrhs, lane, cuda):
     assert np.array_equal(T1[fb], T2[fb], equal_nan=True)
     assert np.array_equal(A1[ok], O.unpack(ap, nm, m, n, V)[ok])
     assert (T1[ok] == 0).all()
+
+
+@pytest.mark.parametrize("m,n,nrhs", [(40, 8, 3), (64, 16, 2), (12, 8, 2), (20, 6, 2)])
+def test_refined_gels_layouts_agree_bitwise(m, n, nrhs, cuda):
+    """The same batch in column-major (tight and padded leading dimensions) and
+    row-major layouts: x, the residual coordinates, iters and berr are
+    bit-identical (both kernels read A and B through the layout's view)."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(5 * m + n)
+    nm, V = 70, 32
+    A, B, _, _ = C.gen_ls_cond(rng, nm, m, n, nrhs)
+    ng = (nm + V - 1) // V
+    out = []
+    for layout, lda, ldb in (("C", m, m), ("C", m + 3, m + 1), ("R", n + 2, nrhs + 1)):
+        row = layout == "R"
+        a = torch.from_numpy(O.pack(A, V, ld=lda, rowmajor=row)).cuda()
+        b = torch.from_numpy(O.pack(B, V, ld=ldb, rowmajor=row, pad_diag=0.0)).cuda()
+        t = torch.zeros(ng * V * n, dtype=torch.float64, device="cuda")
+        it = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+        be = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+        assert cbk_gb300.dgels_refined_compact(layout, "N", m, n, nrhs, a, lda, b, ldb, t, V, nm,
+                                               iters=it, berr=be) == 0
+        torch.cuda.synchronize()
+        out.append((O.unpack(b.cpu().numpy(), nm, m, nrhs, V, ldb, row), it.cpu().numpy(),
+                    be.cpu().numpy()))
+    for X, it, be in out[1:]:
+        assert np.array_equal(X, out[0][0])
+        assert np.array_equal(it, out[0][1]) and np.array_equal(be, out[0][2])
+    assert (out[0][1] >= 0).all()
