@@ -125,7 +125,7 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
     }
 
     cudaError_t err = cudaSuccess;
-    cudaEvent_t start = nullptr;
+    cudaEvent_t start = nullptr, solved = nullptr;
     auto keep = [&](cudaError_t e) {
         if (err == cudaSuccess && e != cudaSuccess) err = e;
         return err == cudaSuccess;
@@ -140,6 +140,7 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
     int lo_prio = 0, hi_prio = 0;
     keep(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
     keep(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    keep(cudaEventCreateWithFlags(&solved, cudaEventDisableTiming));
     if (err == cudaSuccess) keep(cudaEventRecord(start, caller));
     if (err == cudaSuccess &&
         keep(cudaStreamCreateWithPriority(&in, cudaStreamNonBlocking, hi_prio)))
@@ -188,9 +189,13 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
                              cudaMemcpyHostToDevice, in));
         keep(cudaEventRecord(sl.ready, in));
         keep(cudaStreamWaitEvent(sl.s, sl.ready, 0));
+        // the solves run one after another in chunk order: solves that
+        // overlap each finish late, and a slot is free only when its chunk is
+        if (c > 0) keep(cudaStreamWaitEvent(sl.s, solved, 0));
         keep(launch_posv_refined(row, up, n, nrhs, sl.a, ldap, sl.b, ldbp, V, nmc, max_iter, sl.it,
                                  berr ? sl.be : nullptr, sl.ws, sl.s));
         keep(launch_count_negative(sl.it, nmc, sl.cnt, sl.s));
+        keep(cudaEventRecord(solved, sl.s));
         keep(cudaMemcpyAsync(hb + (size_t)g0 * p.gb, sl.b, (size_t)groups * p.gb,
                              cudaMemcpyDeviceToHost, sl.s));
         if (iters)
@@ -216,6 +221,7 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
         if (slot[k].ready) cudaEventDestroy(slot[k].ready);
     }
     if (start) cudaEventDestroy(start);
+    if (solved) cudaEventDestroy(solved);
     return err;
 }
 

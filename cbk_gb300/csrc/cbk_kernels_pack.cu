@@ -143,26 +143,40 @@ PackGeom make_geom(bool row, int m, int n, int lda, long long stride, int ldap, 
 // The referenced triangle of every n x n matrix of `groups` compact groups:
 // run k (a column of a column-major lower / row-major upper triangle from the
 // diagonal on, or of the opposite pair up to the diagonal) is contiguous, so a
-// block copies it with 16-byte moves; dst has src's layout. Either side may
-// be host memory the device can address (pinned): the copy then runs over the
-// host link at its full rate with half the bytes of the whole matrices.
-// The grid is persistent -- two blocks per SM striding over the runs -- so
-// that the copy keeps running beside a solve that fills the rest of the GPU
-// (a grid of one block per run would wait for the solve's blocks to drain).
+// warp copies it with 16-byte moves, four loads in flight per lane before
+// their stores; dst has src's layout. Either side may be host memory the
+// device can address (pinned): the copy then runs over the host link at its
+// full rate with half the bytes of the whole matrices. Over the link a load
+// takes microseconds, so the bytes in flight set the rate, and with four per
+// lane one block per two SMs fills the link. The grid is that small and
+// persistent: it runs beside a solve that fills the rest of the GPU (a grid
+// of one block per run would wait for the solve's blocks to drain), and it
+// takes few of the solve's SM slots (measured: two blocks per SM slowed the
+// solves beside it until they, not the link, set the pace).
 __global__ void __launch_bounds__(256)
     k_tri_copy(const double *__restrict__ src, double *__restrict__ dst, bool from_diag, int n,
                int ld, int V, long groups, long gstride)
 {
+    constexpr int UNROLL = 4;
     const long runs = groups * n;
-    for (long b = blockIdx.x; b < runs; b += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    const long wpb = blockDim.x >> 5;
+    for (long b = blockIdx.x * wpb + (threadIdx.x >> 5); b < runs; b += gridDim.x * wpb) {
         const long g = b / n;
         const int k = (int)(b - g * n);
         const long start = ((long)k * ld + (from_diag ? k : 0)) * V;
         const long len2 = (long)(from_diag ? n - k : k + 1) * V / 2; // V is even
         const double2 *s = reinterpret_cast<const double2 *>(src + g * gstride + start);
         double2 *d = reinterpret_cast<double2 *>(dst + g * gstride + start);
-        for (long i = threadIdx.x; i < len2; i += blockDim.x)
-            d[i] = s[i];
+        for (long i = lane; i < len2; i += 32 * UNROLL) {
+            double2 v[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u)
+                if (i + 32 * u < len2) v[u] = s[i + 32 * u];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u)
+                if (i + 32 * u < len2) d[i + 32 * u] = v[u];
+        }
     }
 }
 
@@ -175,7 +189,7 @@ cudaError_t launch_tri_copy(bool row, bool up, int n, int ld, int V, long groups
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long blocks = std::min<long>(groups * n, 2L * std::max(sms, 1));
+    const long blocks = std::min<long>(groups * n, std::max(sms / 2, 1));
     k_tri_copy<<<(unsigned)blocks, 256, 0, s>>>(src, dst, row == up, n, ld, V, groups,
                                                 (long)ld * n * V);
     return cudaGetLastError();
