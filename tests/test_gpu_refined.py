@@ -124,3 +124,21 @@ def test_refined_argument_checks(cuda):
     assert cbk_gb300.dposv_refined_lwork(8, 1, 32, 64) == 0
     assert cbk_gb300.dposv_refined_lwork(48, 1, 32, 64) == 0  # one warp per matrix, on chip
     assert cbk_gb300.dposv_refined_lwork(70, 1, 32, 64) > 70 * 70 * 4 * 64
+
+
+@pytest.mark.parametrize("n", [8, 16, 24, 48, 70])
+def test_refined_results_independent_of_width(n, cuda):
+    """Each matrix's arithmetic is the same whatever the interleave width: at
+    V = 8, 16 and 64 (blocks of the warp kernel then straddle groups, or hold
+    a group's quarter) x, iters and berr equal V = 32's bit for bit."""
+    rng = np.random.default_rng(400 + n)
+    nm = 150
+    A, _ = C.gen_spd_cond(rng, nm, n)
+    B = rng.standard_normal((nm, n, 1))
+    ref = _run(A, B, 32)
+    assert ref[0] == 0
+    for V in (8, 16, 64):
+        got = _run(A, B, V)
+        assert got[0] == 0
+        assert np.array_equal(got[1], ref[1]), V
+        assert np.array_equal(got[4], ref[4]) and np.array_equal(got[5], ref[5]), V

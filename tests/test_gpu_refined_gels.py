@@ -176,3 +176,30 @@ def test_refined_gels_layouts_agree_bitwise(m, n, nrhs, cuda):
         assert np.array_equal(X, out[0][0])
         assert np.array_equal(it, out[0][1]) and np.array_equal(be, out[0][2])
     assert (out[0][1] >= 0).all()
+
+
+@pytest.mark.parametrize("m,n,nrhs", [(64, 16, 2), (40, 8, 3), (20, 6, 2)])
+def test_refined_gels_independent_of_width(m, n, nrhs, cuda):
+    """x, iters and berr at V = 16 and 64 equal V = 32's bit for bit."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(9 * m + n)
+    nm = 90
+    A, B, _, _ = C.gen_ls_cond(rng, nm, m, n, nrhs)
+    out = []
+    for V in (32, 16, 64):
+        ng = (nm + V - 1) // V
+        a = torch.from_numpy(O.pack(A, V)).cuda()
+        b = torch.from_numpy(O.pack(B, V, pad_diag=0.0)).cuda()
+        t = torch.zeros(ng * V * n, dtype=torch.float64, device="cuda")
+        it = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+        be = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+        assert cbk_gb300.dgels_refined_compact("C", "N", m, n, nrhs, a, m, b, m, t, V, nm,
+                                               iters=it, berr=be) == 0
+        torch.cuda.synchronize()
+        out.append((O.unpack(b.cpu().numpy(), nm, m, nrhs, V), it.cpu().numpy(),
+                    be.cpu().numpy()))
+    for X, it, be in out[1:]:
+        assert np.array_equal(X, out[0][0])
+        assert np.array_equal(it, out[0][1]) and np.array_equal(be, out[0][2])
