@@ -25,6 +25,10 @@ def test_set_get_reset(tune):
     assert tune.tune_get("posv", "d", 47)[1]["threads"] == 0      # per order
     assert tune.tune_set("posv_refined", "d", 48, variant=1) == 0
     assert tune.tune_get("posv_refined", "d", 48)[1]["variant"] == 1
+    # the least squares' kernel choice (0: a warp per matrix, 1: a lane per matrix)
+    assert tune.tune_set("gels_refined", "d", 16, variant=1) == 0
+    assert tune.tune_get("gels_refined", "d", 16)[1]["variant"] == 1
+    assert tune.tune_get("gels_refined", "d", 8)[1]["variant"] == 0
     # orders past 64 share one entry
     assert tune.tune_set("geqrf", "s", 100, threads=64) == 0
     assert tune.tune_get("geqrf", "s", 300)[1]["threads"] == 64
@@ -48,13 +52,16 @@ def test_argument_checks(tune):
     assert tune.autotune("posv", "d", 8, 8, 0, 64)[0] == -5
     assert tune.autotune("posv", "d", 8, 8, 1, 0)[0] == -6
     assert tune.autotune("posv_refined", "s", 8, 8, 1, 64)[0] == -2
+    # the least squares' variant is set, not measured
+    assert tune.autotune("gels_refined", "d", 64, 16, 8, 64)[0] == -1
     assert tune.autotune_at("posv", "d", 8, 8, 1, 64, 48)[0] == -7
     assert tune.autotune_at("nope", "d", 8, 8, 1, 64, 32)[0] == -1
 
 
 def test_save_load_round_trip(tune, tmp_path):
     entries = [("posv", "d", 8, 64, 0, 32), ("posv_refined", "d", 48, 0, 1, 64),
-               ("gels", "s", 16, 256, 0, 128), ("sysvnp", "d", 64, 128, 0, 0)]
+               ("gels", "s", 16, 256, 0, 128), ("sysvnp", "d", 64, 128, 0, 0),
+               ("gels_refined", "d", 16, 0, 1, 0)]
     for e in entries:
         assert tune.tune_set(*e) == 0
     path = str(tmp_path / "tune.txt")
