@@ -783,6 +783,46 @@ def run_config(args):
                     speedup_graph_vs_per_size=tp / tg, gpu_launches=args.steps)
         line["config"]["workload"] = ("dsysvnp_compact, 1048576 matrices, n uniform in 4..48, "
                                       "45 buckets, V=32: one persistent CUDA-graph launch")
+    elif args.config == "c3d":
+        # the headline batches as strided dense column-major arrays (lda = n,
+        # stride n^2): the refined solve reads and writes them in place,
+        # against the compact path on the same matrices
+        per, td_all, tc_all, same = {}, 0.0, 0.0, True
+        for n in SIZES:
+            A, B = gen_batch(n, NM, gen, dev)
+            a0, b0 = A.contiguous(), B.contiguous()
+            ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+            del A, B
+            a, b, ap, bp = a0.clone(), b0.clone(), ap0.clone(), bp0.clone()
+            it = torch.empty(NM, dtype=torch.int32, device=dev)
+
+            def rd():
+                a.copy_(a0)
+                b.copy_(b0)
+
+            def rc():
+                ap.copy_(ap0)
+                bp.copy_(bp0)
+            td, _ = timed(lambda: cbk.check("batched", cbk.dposv_refined_batched(
+                "L", n, NRHS, a, n, n * n, b, n, n * NRHS, NM, 10, it)) or 1, rd, args.steps,
+                args.warmup)
+            tc, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
+                "C", "L", n, NRHS, ap, n, bp, n, V, NM, 10, it)) or 1, rc, args.steps,
+                args.warmup)
+            same = same and torch.equal(b.view(NM, n), x_dense(bp, n, NM).view(NM, n))
+            per[str(n)] = {"dense_ms": td, "compact_ms": tc}
+            td_all += td
+            tc_all += tc
+            del a0, b0, ap0, bp0, a, b, ap, bp
+        line.update(metric="mixed-precision dposv on strided dense batches solves/s, n=8-48",
+                    value=NM * len(SIZES) / (td_all * 1e-3), unit=UNIT, ms_per_step=td_all,
+                    dtype="f32 factor + f64 refinement (f64 results)",
+                    data="synthetic: the headline's matrices (seed 0x5EED), dense column-major",
+                    compact={"value": NM * len(SIZES) / (tc_all * 1e-3), "ms_per_step": tc_all},
+                    per_n=per, x_bit_identical_to_compact=bool(same),
+                    gpu_launches=len(SIZES) * args.steps)
+        line["config"]["workload"] = ("dposv_refined_batched: n in {8,16,32,48}, 262144 matrices "
+                                      "each, A column-major lda = n, stride n^2, nrhs = 1")
     elif args.config == "c5":
         m, n, nrhs, nm = 64, 16, 8, 131072
         ap0, bp0, Ad, Bd = ls_batch(m, n, nrhs, nm, dev)
@@ -829,7 +869,7 @@ def main():
                     help="keep the built-in launch shapes instead of autotuning them first")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5"), default="c3",
+    ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5", "c3d"), default="c3",
                     help="c3 (default) is the headline; the others print their own line")
     ap.add_argument("--case", nargs=3, metavar=("KIND", "N", "NM"),
                     help="no timing: solve one batch (refined|plain, order N, NM matrices) "

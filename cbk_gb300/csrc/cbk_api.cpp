@@ -240,6 +240,32 @@ int posv_refined(char layout, char uplo, int n, int nrhs, double *ap, int ldap, 
                                            iters, berr, work, s));
 }
 
+// The refined solve on a strided dense batch: matrix k's A at a + k stride_a
+// (column-major, leading dimension lda), its B at b + k stride_b. That is
+// the compact layout at V = 1 with the caller's group strides, so the kernels
+// read and write the dense arrays directly (no pack or unpack pass).
+int posv_refined_batched(char uplo, int n, int nrhs, double *a, int lda, long long stride_a,
+                         double *b, int ldb, long long stride_b, int nm, int max_iter, int *iters,
+                         double *berr, void *work, long long lwork, cudaStream_t s)
+{
+    const bool lo = opt(uplo, 'L'), up = opt(uplo, 'U');
+    if (!lo && !up) return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (lda < max1(n)) return -5;
+    if (stride_a < (long long)lda * n) return -6;
+    if (ldb < max1(n)) return -8;
+    if (stride_b < (long long)ldb * nrhs) return -9;
+    if (nm < 0) return -10;
+    if (max_iter < 0) return -11;
+    if (n == 0 || nm == 0 || nrhs == 0) return 0;
+    const size_t need = posv_refined_lwork(n, nrhs, 1, nm);
+    if (need > 0 && (work == nullptr || lwork < (long long)need)) return -15;
+    return cuda_status(launch_posv_refined(false, up, n, nrhs, a, lda, b, ldb, 1, nm, max_iter,
+                                           iters, berr, work, s, (size_t)stride_a,
+                                           (size_t)stride_b));
+}
+
 int gels_refined(char layout, char trans, int m, int n, int nrhs, double *ap, int ldap, double *bp,
                  int ldbp, double *taup, int V, int nm, int max_iter, int *iters, double *berr,
                  void *work, long long lwork, cudaStream_t s)
@@ -483,6 +509,22 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
 {
     return posv_refined(layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter, iters, berr,
                         work, lwork, S(st));
+}
+
+long long cbk_cuda_dposv_refined_batched_lwork(int n, int nrhs, int nm)
+{
+    if (n < 0 || nrhs < 0 || nm < 0) return -1;
+    return (long long)posv_refined_lwork(n, nrhs, 1, nm);
+}
+
+int cbk_cuda_dposv_refined_batched_async(char uplo, int n, int nrhs, double *a, int lda,
+                                         long long stride_a, double *b, int ldb,
+                                         long long stride_b, int nm, int max_iter, int *iters,
+                                         double *berr, void *work, long long lwork,
+                                         cbk_stream_t st)
+{
+    return posv_refined_batched(uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm, max_iter,
+                                iters, berr, work, lwork, S(st));
 }
 
 long long cbk_cuda_dposv_refined_compact_host_lwork(char layout, int n, int nrhs, int ldap,

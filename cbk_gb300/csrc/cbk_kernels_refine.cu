@@ -410,10 +410,11 @@ size_t posv_refined_lwork(int n, int nrhs, int V, int nm)
 
 cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                 double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
-                                double *berr, void *work, cudaStream_t s)
+                                double *berr, void *work, cudaStream_t s, size_t sa_, size_t sb_)
 {
     const long ng = ((long)nm + V - 1) / V;
-    const size_t sa = gstride(row, ldap, n, n, V), sb = gstride(row, ldbp, n, nrhs, V);
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, n, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, n, nrhs, V);
     const RefineOut out{iters, berr, nm, max_iter};
     // the lane-per-matrix variants are compiled for at most 128 threads
     const int th = std::min(threads_for(R_POSV_REFINED, n, sizeof(double)), 128);
@@ -436,7 +437,7 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
     }
     if (posv_refined_warp_ok(n))
         return launch_posv_refined_warp(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter,
-                                        iters, berr, s);
+                                        iters, berr, s, sa, sb);
     const size_t lanes = (size_t)ng * V;
     char *base = static_cast<char *>(work);
     RefineWork w;

@@ -720,7 +720,8 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
 
 template <int N, int WPB, int MINB>
 cudaError_t launch_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
-                        int ldbp, int V, int nm, const WarpOut &out, cudaStream_t s)
+                        int ldbp, int V, int nm, const WarpOut &out, cudaStream_t s, size_t sa,
+                        size_t sb)
 {
     const long ng = ((long)nm + V - 1) / V;
     const long nlanes = ng * V;
@@ -733,8 +734,7 @@ cudaError_t launch_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap
     }
     const unsigned blocks = (unsigned)((nlanes + WPB - 1) / WPB);
     k_posv_refined_warp<N, WPB, MINB><<<blocks, WPB * 32, smem, s>>>(
-        row, up, n, nrhs, ap, ldap, bp, ldbp, V, nlanes, gstride(row, ldap, n, n, V),
-        gstride(row, ldbp, n, nrhs, V), out);
+        row, up, n, nrhs, ap, ldap, bp, ldbp, V, nlanes, sa, sb, out);
     return cudaGetLastError();
 }
 
@@ -748,9 +748,12 @@ bool posv_refined_warp_ok(int n)
 
 cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                      double *bp, int ldbp, int V, int nm, int max_iter,
-                                     int *iters, double *berr, cudaStream_t s)
+                                     int *iters, double *berr, cudaStream_t s, size_t sa_,
+                                     size_t sb_)
 {
     const WarpOut out{iters, berr, nm, max_iter};
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, n, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, n, nrhs, V);
     // four matrices per block (the staging loads then fill 32-byte sectors);
     // the order is padded to a multiple of 8, and the last template argument
     // caps the registers for the resident blocks wanted (measured: at n = 32
@@ -758,8 +761,9 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
     // Variant 1 asks for one block more per SM (fewer registers per thread).
     const bool more = variant_for(R_POSV_REFINED, n, 8) == 1;
 #define CBK_WARP(N, B)                                                                             \
-    return more ? launch_warp<N, 4, B + 1>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s)    \
-                : launch_warp<N, 4, B>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s)
+    return more ? launch_warp<N, 4, B + 1>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s, sa, \
+                                           sb)                                                     \
+                : launch_warp<N, 4, B>(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, out, s, sa, sb)
     switch ((n + 7) / 8) {
     case 3: CBK_WARP(24, 6);
     case 4: CBK_WARP(32, 7);

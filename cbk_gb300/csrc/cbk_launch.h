@@ -88,9 +88,12 @@ cudaError_t launch_unpack(bool row, int m, int n, const T *ap, int ldap, T *a, i
 
 // mixed-precision SPD solve (cbk_kernels_refine.cu)
 size_t posv_refined_lwork(int n, int nrhs, int V, int nm);
+// sa_ / sb_: the scalars from one group of A / B to the next; 0 takes the
+// compact layout's own (a dense batch is V = 1 with the caller's strides)
 cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                 double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
-                                double *berr, void *work, cudaStream_t s);
+                                double *berr, void *work, cudaStream_t s, size_t sa_ = 0,
+                                size_t sb_ = 0);
 // mixed-precision least squares (cbk_kernels_refine_gels.cu)
 size_t gels_refined_lwork(int m, int n, int nrhs, int V, int nm);
 int gels_refined_nmax();
@@ -114,7 +117,8 @@ cudaError_t launch_bucketed(bool ldlt, bool row, bool up, int nrhs, int nbuckets
 bool posv_refined_warp_ok(int n);
 cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap,
                                      double *bp, int ldbp, int V, int nm, int max_iter,
-                                     int *iters, double *berr, cudaStream_t s);
+                                     int *iters, double *berr, cudaStream_t s, size_t sa_ = 0,
+                                     size_t sb_ = 0);
 
 // the refined solve on host-memory batches, copies pipelined with the solves
 // (cbk_host.cpp); dwork: device workspace of posv_refined_host_lwork bytes

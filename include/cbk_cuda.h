@@ -250,6 +250,26 @@ int cbk_cuda_dposv_refined_compact_async(char layout, char uplo, int n, int nrhs
                                          int max_iter, int *iters, double *berr, void *work,
                                          long long lwork, cbk_stream_t stream);
 
+/* The same solve on a strided dense batch, the layout of cuBLAS/cuSOLVER
+ * batched routines: matrix k's A is column-major at a + k*stride_a with
+ * leading dimension lda (the uplo triangle referenced), its B at
+ * b + k*stride_b with leading dimension ldb. No reference entry point: the
+ * reference's callers pack into the compact layout first
+ * (tests/test_compact_util.hpp:468-531); here the kernels read and write
+ * the dense arrays directly, and each matrix's results are bit-identical to
+ * the compact entry point's for the same matrix. Returns 0, -1 uplo, -2 n,
+ * -3 nrhs, -5 lda < max(1,n), -6 stride_a < lda*n, -8 ldb < max(1,n),
+ * -9 stride_b < ldb*nrhs, -10 nm, -11 max_iter, -15 work/lwork below
+ * cbk_cuda_dposv_refined_batched_lwork(n, nrhs, nm) (0 for n <= 64; -1 for
+ * a negative argument), or CBK_CUDA_ERROR_BASE + a CUDA error. iters, berr
+ * and the fallback are as for the compact entry point. */
+long long cbk_cuda_dposv_refined_batched_lwork(int n, int nrhs, int nm);
+int cbk_cuda_dposv_refined_batched_async(char uplo, int n, int nrhs, double *a, int lda,
+                                         long long stride_a, double *b, int ldb,
+                                         long long stride_b, int nm, int max_iter, int *iters,
+                                         double *berr, void *work, long long lwork,
+                                         cbk_stream_t stream);
+
 /* The same solve on batches in HOST memory (ap, bp, iters, berr are host
  * pointers; pinned memory lets the copies overlap the solves). No reference
  * entry point: the reference's own calling convention -- every array on the

@@ -155,3 +155,24 @@ def test_refined_host_entry_validates_before_any_device_work():
     assert big == lw("C", 48, 1, 48, 48, 32, 2 * 10 ** 6)
     assert big < 3 * 300 * 32 * 48 * 48 * 8 + (64 << 20)
     assert lw("C", 8, 1, 8, 8, 32, 10 ** 7) == lw("C", 8, 1, 8, 8, 32, 2 * 10 ** 7)
+
+
+def test_refined_batched_argument_checks():
+    """The strided dense batch entry point: -j in argument order, quick
+    returns, the workspace query (CPU only: no device work)."""
+    import cbk_gb300
+    f = cbk_gb300.dposv_refined_batched
+    assert f("X", 8, 1, None, 8, 64, None, 8, 8, 10) == -1
+    assert f("L", -1, 1, None, 8, 64, None, 8, 8, 10) == -2
+    assert f("L", 8, -1, None, 8, 64, None, 8, 8, 10) == -3
+    assert f("L", 8, 1, None, 7, 64, None, 8, 8, 10) == -5
+    assert f("L", 8, 1, None, 8, 63, None, 8, 8, 10) == -6
+    assert f("L", 8, 1, None, 8, 64, None, 7, 8, 10) == -8
+    assert f("L", 8, 2, None, 8, 64, None, 8, 15, 10) == -9
+    assert f("L", 8, 1, None, 8, 64, None, 8, 8, -1) == -10
+    assert f("L", 8, 1, None, 8, 64, None, 8, 8, 10, max_iter=-1) == -11
+    assert f("L", 80, 1, None, 80, 6400, None, 80, 80, 10, work=0, lwork=0) == -15
+    assert f("L", 8, 0, None, 8, 64, None, 8, 8, 10) == 0
+    assert f("U", 0, 1, None, 1, 0, None, 1, 1, 10) == 0
+    lw = cbk_gb300.dposv_refined_batched_lwork
+    assert lw(48, 1, 1000) == 0 and lw(80, 1, 100) > 0 and lw(-1, 1, 1) == -1

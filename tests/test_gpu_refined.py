@@ -142,3 +142,57 @@ def test_refined_results_independent_of_width(n, cuda):
         assert got[0] == 0
         assert np.array_equal(got[1], ref[1]), V
         assert np.array_equal(got[4], ref[4]) and np.array_equal(got[5], ref[5]), V
+
+
+def _dense(M, ld, stride, fill):
+    """(nm, rows, cols) -> a flat strided column-major batch, padding = fill."""
+    nm, rows, cols = M.shape
+    out = np.full(nm * stride, fill)
+    for k in range(nm):
+        out[k * stride:k * stride + cols * ld].reshape(cols, ld)[:, :rows] = M[k].T
+    return out
+
+
+@pytest.mark.parametrize("n,nrhs", [(8, 1), (16, 2), (24, 1), (48, 1), (70, 1)])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_refined_batched_equals_compact(n, nrhs, uplo, cuda):
+    """A strided dense batch (padded lda, ldb and strides) through
+    dposv_refined_batched gives each matrix's x, iters, berr -- and, for a
+    matrix that falls back, the FP64 factor -- bit-identical to the compact
+    entry point's; the padding is untouched."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(70 * n + nrhs)
+    nm = 75
+    A, _ = C.gen_spd_cond(rng, nm, n)
+    A[5] *= 1e42                                    # falls back (iters -2)
+    B = rng.standard_normal((nm, n, nrhs))
+    info, X, a1, a0, it, be = _run(A, B, 32, "C", uplo)
+    assert info == 0 and it[5] == -2
+    lda, ldb = n + 3, n + 1
+    sa, sb = lda * n + 5, ldb * nrhs + 2
+    ad = torch.from_numpy(_dense(A, lda, sa, 7.0)).cuda()
+    bd = torch.from_numpy(_dense(B, ldb, sb, 9.0)).cuda()
+    itd = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    bed = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+    assert cbk_gb300.dposv_refined_batched(uplo, n, nrhs, ad, lda, sa, bd, ldb, sb, nm,
+                                           iters=itd, berr=bed) == 0
+    torch.cuda.synchronize()
+    bh, ah = bd.cpu().numpy(), ad.cpu().numpy()
+    Xd = np.stack([bh[k * sb:k * sb + nrhs * ldb].reshape(nrhs, ldb)[:, :n].T for k in range(nm)])
+    assert np.array_equal(Xd, X)
+    assert np.array_equal(itd.cpu().numpy(), it)
+    assert np.array_equal(bed.cpu().numpy(), be, equal_nan=True)
+    # padding untouched: B's and A's gaps and the rows past n
+    mb = _dense(np.zeros_like(B), ldb, sb, 1.0) == 1.0
+    assert (bh[mb] == 9.0).all()
+    ma = _dense(np.zeros_like(A), lda, sa, 1.0) == 1.0
+    assert (ah[ma] == 7.0).all()
+    # the fallen matrix holds the FP64 factor, as in the compact layout; the
+    # others their input
+    Ad = np.stack([ah[k * sa:k * sa + n * lda].reshape(n, lda)[:, :n].T for k in range(nm)])
+    Ac = O.unpack(a1, nm, n, n, 32)
+    assert np.array_equal(Ad[5], Ac[5])
+    ok = it >= 0
+    assert np.array_equal(Ad[ok], A[ok])
