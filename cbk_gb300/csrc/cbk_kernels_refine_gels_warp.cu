@@ -7,26 +7,25 @@
 // One thread per matrix keeps the FP32 QR in a global workspace and waits on
 // memory at every step, and a warp of 32 matrices runs until its slowest
 // lane converges. Here the 32 lanes share one matrix:
-//   * the block's four matrices are staged into shared memory with
-//     asynchronous copies (coalesced across the block), then lane l takes
-//     rows l and l + 32 of A into registers in FP64 (the residuals) and in
-//     FP32 (the QR); rows past m are zero, which changes no result;
-//   * the FP32 Householder QR works on the register rows: each column's norm
-//     and each reflector application is a warp sum; R (rows 0 .. n-1, lanes
-//     0 .. n-1) is copied to shared memory for the triangular solves, which
-//     run as n broadcast steps;
-//   * per refinement step f = b - r - A x is row-parallel (x broadcast from
-//     shared memory), and g = A^T r is a per-lane partial sum of the n
-//     columns reduced across the warp by recursive halving: each exchange
-//     sends half of the values still held, so the n column sums cost n FP64
-//     additions per lane in all (a plain butterfly per column would cost
-//     5 n).
-// The FP32 correction uses the thin Q1 formed explicitly (m x n, in
-// registers) and R^-1 formed explicitly (shared memory): with t = Q1^T f -
-// R^-T g, dx = R^-1 t and dr = f - Q1 t, so a step costs two column sums and
-// three broadcast products instead of 2n sequential reflector applications;
-// the reflectors themselves are applied once per right-hand side, for the
-// residual coordinates returned in B(n:m).
+//   * the block's four matrices are staged into shared memory in FP64 with
+//     asynchronous copies (coalesced across the block), column-major with
+//     rows past m zero (which changes no result); the FP64 residuals read A
+//     from there at every step;
+//   * lane l takes rows l and l + 32 of the FP32 copy into registers, and
+//     the FP32 Householder QR works on these rows: each column's norm and
+//     each reflector application is a warp sum (the trailing columns' sums
+//     interleaved); the factored columns (R and the reflectors) are stored
+//     to shared memory;
+//   * the thin Q1 (m x n, in registers) and R^-1 (shared memory) are formed
+//     explicitly once per matrix. A correction is then t = Q1^T f - R^-T g,
+//     dx = R^-1 t and dr = f - Q1 t: two column sums and three broadcast
+//     products instead of 2n dependent reflector applications. The
+//     reflectors themselves are applied once per right-hand side, for the
+//     residual coordinates returned in B(n:m);
+//   * per step f = b - r - A x is row-parallel (x broadcast from shared
+//     memory), and g = -A^T r takes 32/n lanes per column, each over
+//     interleaved rows, then log2(32/n) shuffle-adds: the FP64 work is the
+//     FMAs alone, with no reduction tree per column.
 // The FP64 work is the lane kernel's (2 m n fused multiply-adds per
 // right-hand side and step, less the first step's f, see below), with every
 // lane of the warp busy until its one matrix converges.
