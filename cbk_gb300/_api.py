@@ -121,6 +121,53 @@ def dposv_refined_batched(uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm,
 __all__ += ["dposv_refined_batched", "dposv_refined_batched_lwork"]
 
 
+def dgels_refined_batched_lwork(m: int, n: int, nrhs: int, nm: int) -> int:
+    """Workspace bytes of dgels_refined_batched (-1: illegal argument)."""
+    import ctypes
+
+    from ._abi import lib
+    f = lib().cbk_cuda_dgels_refined_batched_lwork
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_int] * 4
+    return f(m, n, nrhs, nm)
+
+
+def dgels_refined_batched(trans, m, n, nrhs, a, lda, stride_a, b, ldb, stride_b, tau, nm,
+                          max_iter=10, iters=None, berr=None, work=None, lwork=None,
+                          stream=None):
+    """The mixed-precision least squares on a strided dense batch: matrix k's
+    A column-major at a + k stride_a, B at b + k stride_b, tau at tau + k n.
+    Results per matrix equal dgels_refined_compact's."""
+    import ctypes
+
+    from ._abi import _ptr, _stream, lib
+    need = dgels_refined_batched_lwork(m, n, nrhs, nm) if min(m, n, nm) > 0 else 0
+    if work is None and need > 0:
+        import torch
+        work = torch.empty(need, dtype=torch.uint8, device="cuda")
+    f = lib().cbk_cuda_dgels_refined_batched_async
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int,
+                  ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+                  ctypes.c_void_p]
+
+    def raw(t):
+        if t is None or isinstance(t, int):
+            return t
+        return t.data_ptr()
+    wbytes = lwork if lwork is not None else (work.numel() * work.element_size()
+                                              if work is not None and not isinstance(work, int)
+                                              else 0)
+    return f(trans.encode(), m, n, nrhs, _ptr(a, "d"), lda, stride_a, _ptr(b, "d"), ldb,
+             stride_b, _ptr(tau, "d"), nm, max_iter, raw(iters), raw(berr), raw(work), wbytes,
+             _stream(stream) if (a is not None and not isinstance(a, int)) or stream else None)
+
+
+__all__ += ["dgels_refined_batched", "dgels_refined_batched_lwork"]
+
+
 def dposv_refined_host_lwork(layout: str, n: int, nrhs: int, ldap: int, ldbp: int, V: int,
                              nm: int) -> int:
     """Device workspace bytes of dposv_refined_compact_host (-1: illegal argument)."""

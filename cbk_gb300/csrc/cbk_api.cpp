@@ -266,6 +266,35 @@ int posv_refined_batched(char uplo, int n, int nrhs, double *a, int lda, long lo
                                            (size_t)stride_b));
 }
 
+// The refined least squares on a strided dense batch (A m x n at
+// a + k stride_a, B m x nrhs at b + k stride_b, column-major; tau n per
+// matrix at tau + k n): the compact layout at V = 1 with these strides.
+int gels_refined_batched(char trans, int m, int n, int nrhs, double *a, int lda,
+                         long long stride_a, double *b, int ldb, long long stride_b, double *tau,
+                         int nm, int max_iter, int *iters, double *berr, void *work,
+                         long long lwork, cudaStream_t s)
+{
+    if (!opt(trans, 'N')) return -1; // the refined path solves A X = B
+    if (m < 0) return -2;
+    if (n < 0 || n > m || n > gels_refined_nmax()) return -3;
+    if (nrhs < 0) return -4;
+    if (lda < max1(m)) return -6;
+    if (stride_a < (long long)lda * n) return -7;
+    if (ldb < max1(m)) return -9;
+    if (stride_b < (long long)ldb * nrhs) return -10;
+    if (nm < 0) return -12;
+    if (max_iter < 0) return -13;
+    if (nrhs == 0 || nm == 0 || m == 0) return 0;
+    if (n == 0)
+        return cuda_status(
+            launch_zero<double>(false, m, nrhs, b, ldb, 1, nm, s, (size_t)stride_b));
+    const size_t need = gels_refined_lwork(m, n, nrhs, 1, nm);
+    if (work == nullptr || lwork < (long long)need) return -17;
+    return cuda_status(launch_gels_refined(false, m, n, nrhs, a, lda, b, ldb, tau, 1, nm,
+                                           max_iter, iters, berr, work, s, (size_t)stride_a,
+                                           (size_t)stride_b));
+}
+
 int gels_refined(char layout, char trans, int m, int n, int nrhs, double *ap, int ldap, double *bp,
                  int ldbp, double *taup, int V, int nm, int max_iter, int *iters, double *berr,
                  void *work, long long lwork, cudaStream_t s)
@@ -583,6 +612,22 @@ int cbk_cuda_dgels_refined_compact_async(char layout, char trans, int m, int n, 
 {
     return gels_refined(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, max_iter,
                         iters, berr, work, lwork, S(st));
+}
+
+long long cbk_cuda_dgels_refined_batched_lwork(int m, int n, int nrhs, int nm)
+{
+    if (m < 0 || n < 0 || nrhs < 0 || nm < 0) return -1;
+    return (long long)gels_refined_lwork(m, n, nrhs, 1, nm);
+}
+
+int cbk_cuda_dgels_refined_batched_async(char trans, int m, int n, int nrhs, double *a, int lda,
+                                         long long stride_a, double *b, int ldb,
+                                         long long stride_b, double *tau, int nm, int max_iter,
+                                         int *iters, double *berr, void *work, long long lwork,
+                                         cbk_stream_t st)
+{
+    return gels_refined_batched(trans, m, n, nrhs, a, lda, stride_a, b, ldb, stride_b, tau, nm,
+                                max_iter, iters, berr, work, lwork, S(st));
 }
 
 int cbk_cuda_dsysvnp_compact_bucketed_async(char layout, char uplo, int nrhs, int nbuckets,

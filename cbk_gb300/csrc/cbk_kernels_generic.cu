@@ -112,12 +112,12 @@ __global__ void k_gels(bool row, bool tall, bool overdet, int p, int q, int nrhs
 
 template <typename T>
 cudaError_t launch_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, int nm,
-                        cudaStream_t s)
+                        cudaStream_t s, size_t sb_)
 {
     const long ng = groups_of(nm, V);
     const int th = threads_for(R_ZERO, rows, sizeof(T));
     k_zero<T><<<blocks_for(ng, V, th), th, 0, s>>>(row, rows, cols, bp, ldbp, V, ng,
-                                                   gstride(row, ldbp, rows, cols, V));
+                                                   sb_ ? sb_ : gstride(row, ldbp, rows, cols, V));
     return cudaGetLastError();
 }
 
@@ -239,7 +239,7 @@ cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, in
 }
 
 #define CBK_INSTANTIATE(T)                                                                        \
-    template cudaError_t launch_zero<T>(bool, int, int, T *, int, int, int, cudaStream_t);         \
+    template cudaError_t launch_zero<T>(bool, int, int, T *, int, int, int, cudaStream_t, size_t); \
     template cudaError_t launch_factor<T>(bool, bool, bool, int, T *, int, int, int,               \
                                           cudaStream_t);                                          \
     template cudaError_t launch_sym_solve_generic<T>(bool, bool, bool, bool, int, int, T *, int,   \

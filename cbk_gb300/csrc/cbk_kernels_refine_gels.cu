@@ -218,12 +218,14 @@ int gels_refined_nmax()
 
 cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, int ldap, double *bp,
                                 int ldbp, double *taup, int V, int nm, int max_iter, int *iters,
-                                double *berr, void *work, cudaStream_t s)
+                                double *berr, void *work, cudaStream_t s, size_t sa_, size_t sb_)
 {
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, m, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, m, nrhs, V);
     // variant 0: one warp per matrix where it is compiled; 1: one lane per matrix
     if (gels_refined_warp_ok(m, n) && variant_for(R_GELS_REFINED, n, 8) == 0)
         return launch_gels_refined_warp(row, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
-                                        max_iter, iters, berr, s);
+                                        max_iter, iters, berr, s, sa, sb);
     const long ng = ((long)nm + V - 1) / V;
     const size_t lanes = (size_t)ng * V;
     char *base = static_cast<char *>(work);
@@ -237,8 +239,7 @@ cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, in
     w.r = reinterpret_cast<double *>(base);
     const int th = 128;
     k_gels_refined<<<(unsigned)((lanes + th - 1) / th), th, 0, s>>>(
-        row, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, ng, gstride(row, ldap, m, n, V),
-        gstride(row, ldbp, m, nrhs, V), w, max_iter, iters, berr, nm);
+        row, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, ng, sa, sb, w, max_iter, iters, berr, nm);
     return cudaGetLastError();
 }
 

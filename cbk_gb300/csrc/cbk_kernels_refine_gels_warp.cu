@@ -525,7 +525,8 @@ namespace {
 
 template <int MR, int N, int MINB>
 cudaError_t launch_warp_gels(bool row, int m, int nrhs, double *ap, int ldap, double *bp, int ldbp,
-                             double *taup, int V, int nm, GelsOut out, cudaStream_t s)
+                             double *taup, int V, int nm, GelsOut out, cudaStream_t s, size_t sa,
+                             size_t sb)
 {
     constexpr int WPB = 4;
     const size_t smem = (size_t)WPB * GW<MR, N>::BYTES;
@@ -540,8 +541,7 @@ cudaError_t launch_warp_gels(bool row, int m, int nrhs, double *ap, int ldap, do
     const long total = ng * V;
     const unsigned blocks = (unsigned)((total + WPB - 1) / WPB);
     k_gels_refined_warp<MR, N, WPB, MINB><<<blocks, 32 * WPB, smem, s>>>(
-        row, m, nrhs, ap, ldap, bp, ldbp, taup, V, total, gstride(row, ldap, m, N, V),
-        gstride(row, ldbp, m, nrhs, V), out);
+        row, m, nrhs, ap, ldap, bp, ldbp, taup, V, total, sa, sb, out);
     return cudaGetLastError();
 }
 
@@ -554,19 +554,22 @@ bool gels_refined_warp_ok(int m, int n)
 
 cudaError_t launch_gels_refined_warp(bool row, int m, int n, int nrhs, double *ap, int ldap,
                                      double *bp, int ldbp, double *taup, int V, int nm,
-                                     int max_iter, int *iters, double *berr, cudaStream_t s)
+                                     int max_iter, int *iters, double *berr, cudaStream_t s,
+                                     size_t sa_, size_t sb_)
 {
     const GelsOut out{iters, berr, nm, max_iter};
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, m, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, m, nrhs, V);
     if (n == 16)
         return m <= 32 ? launch_warp_gels<1, 16, 4>(row, m, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
-                                                    out, s)
+                                                    out, s, sa, sb)
                        : launch_warp_gels<2, 16, 3>(row, m, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
-                                                    out, s);
+                                                    out, s, sa, sb);
     if (n == 8)
         return m <= 32 ? launch_warp_gels<1, 8, 4>(row, m, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
-                                                   out, s)
+                                                   out, s, sa, sb)
                        : launch_warp_gels<2, 8, 4>(row, m, nrhs, ap, ldap, bp, ldbp, taup, V, nm,
-                                                   out, s);
+                                                   out, s, sa, sb);
     return cudaErrorInvalidValue;
 }
 

@@ -37,7 +37,7 @@ enum Routine {
 // every group of a rows x cols batch := 0
 template <typename T>
 cudaError_t launch_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, int nm,
-                        cudaStream_t s);
+                        cudaStream_t s, size_t sb_ = 0);
 
 // potrf (ldlt = false) / sytrfnp (ldlt = true) of the named triangle
 template <typename T>
@@ -101,10 +101,12 @@ int gels_refined_nmax();
 bool gels_refined_warp_ok(int m, int n);
 cudaError_t launch_gels_refined_warp(bool row, int m, int n, int nrhs, double *ap, int ldap,
                                      double *bp, int ldbp, double *taup, int V, int nm,
-                                     int max_iter, int *iters, double *berr, cudaStream_t s);
+                                     int max_iter, int *iters, double *berr, cudaStream_t s,
+                                     size_t sa = 0, size_t sb = 0);
 cudaError_t launch_gels_refined(bool row, int m, int n, int nrhs, double *ap, int ldap, double *bp,
                                 int ldbp, double *taup, int V, int nm, int max_iter, int *iters,
-                                double *berr, void *work, cudaStream_t s);
+                                double *berr, void *work, cudaStream_t s, size_t sa_ = 0,
+                                size_t sb_ = 0);
 
 // one persistent launch over a table of single-order compact buckets
 // (cbk_kernels_bucketed.cu); work holds the 8-byte item counter

@@ -328,6 +328,23 @@ int cbk_cuda_dgels_refined_compact_async(char layout, char trans, int m, int n, 
                                          double *berr, void *work, long long lwork,
                                          cbk_stream_t stream);
 
+/* The same least squares on a strided dense batch: matrix k's A (m x n) is
+ * column-major at a + k*stride_a with leading dimension lda, its B (m x nrhs)
+ * at b + k*stride_b with leading dimension ldb, its n tau values at
+ * tau + k*n. No reference entry point (the reference's callers pack first);
+ * each matrix's results are bit-identical to the compact entry point's.
+ * Returns 0, -1 trans (only 'N'), -2 m, -3 n (0 <= n <= min(m, 64)), -4 nrhs,
+ * -6 lda < max(1,m), -7 stride_a < lda*n, -9 ldb < max(1,m),
+ * -10 stride_b < ldb*nrhs, -12 nm, -13 max_iter, -17 work/lwork below
+ * cbk_cuda_dgels_refined_batched_lwork(m, n, nrhs, nm) (-1 for a negative
+ * argument), or CBK_CUDA_ERROR_BASE + a CUDA error. n = 0 sets B to zero. */
+long long cbk_cuda_dgels_refined_batched_lwork(int m, int n, int nrhs, int nm);
+int cbk_cuda_dgels_refined_batched_async(char trans, int m, int n, int nrhs, double *a, int lda,
+                                         long long stride_a, double *b, int ldb,
+                                         long long stride_b, double *tau, int nm, int max_iter,
+                                         int *iters, double *berr, void *work, long long lwork,
+                                         cbk_stream_t stream);
+
 /* Batches of uneven orders in one persistent launch. No reference counterpart:
  * the reference takes one order per call (?sysvnp_compact, ?posv_compact), so
  * a mixed batch is one call per order. Here the caller groups the matrices by

@@ -176,3 +176,28 @@ def test_refined_batched_argument_checks():
     assert f("U", 0, 1, None, 1, 0, None, 1, 1, 10) == 0
     lw = cbk_gb300.dposv_refined_batched_lwork
     assert lw(48, 1, 1000) == 0 and lw(80, 1, 100) > 0 and lw(-1, 1, 1) == -1
+
+
+def test_refined_gels_batched_argument_checks():
+    """The least squares' strided dense entry point: -j in argument order
+    (CPU only: every row returns before device work)."""
+    import cbk_gb300
+
+    def f(*a, **k):
+        k.setdefault("work", 0)
+        k.setdefault("lwork", 0)
+        return cbk_gb300.dgels_refined_batched(*a, **k)
+    assert f("T", 8, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -1
+    assert f("N", -1, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -2
+    assert f("N", 8, 9, 1, None, 8, 72, None, 8, 8, None, 10) == -3
+    assert f("N", 80, 70, 1, None, 80, 5600, None, 80, 80, None, 10) == -3
+    assert f("N", 8, 4, -1, None, 8, 32, None, 8, 8, None, 10) == -4
+    assert f("N", 8, 4, 1, None, 7, 32, None, 8, 8, None, 10) == -6
+    assert f("N", 8, 4, 1, None, 8, 31, None, 8, 8, None, 10) == -7
+    assert f("N", 8, 4, 1, None, 8, 32, None, 7, 8, None, 10) == -9
+    assert f("N", 8, 4, 2, None, 8, 32, None, 8, 15, None, 10) == -10
+    assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, -1) == -12
+    assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, 10, max_iter=-1) == -13
+    assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -17
+    assert f("N", 8, 4, 0, None, 8, 32, None, 8, 8, None, 10) == 0
+    assert cbk_gb300.dgels_refined_batched_lwork(-1, 1, 1, 1) == -1

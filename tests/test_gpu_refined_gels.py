@@ -203,3 +203,69 @@ def test_refined_gels_independent_of_width(m, n, nrhs, cuda):
     for X, it, be in out[1:]:
         assert np.array_equal(X, out[0][0])
         assert np.array_equal(it, out[0][1]) and np.array_equal(be, out[0][2])
+
+
+def _dense(M, ld, stride, fill):
+    nm, rows, cols = M.shape
+    out = np.full(nm * stride, fill)
+    for k in range(nm):
+        out[k * stride:k * stride + cols * ld].reshape(cols, ld)[:, :rows] = M[k].T
+    return out
+
+
+def _undense(buf, nm, rows, cols, ld, stride):
+    return np.stack([buf[k * stride:k * stride + cols * ld].reshape(cols, ld)[:, :rows].T
+                     for k in range(nm)])
+
+
+@pytest.mark.parametrize("m,n,nrhs", [(64, 16, 3), (40, 8, 2), (20, 6, 2)])
+def test_refined_gels_batched_equals_compact(m, n, nrhs, cuda):
+    """A strided dense batch (padded lda, ldb, strides) through
+    dgels_refined_batched: B (x and the residual coordinates), iters, berr,
+    and for a matrix that falls back its FP64 QR and tau, bit-identical to
+    the compact entry point's; padding untouched; n = 0 sets B to zero."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(31 * m + n)
+    nm, V = 70, 32
+    A, B, _, _ = C.gen_ls_cond(rng, nm, m, n, nrhs)
+    A[4] *= 1e42                                   # falls back (iters -2)
+    ng = (nm + V - 1) // V
+    a1 = torch.from_numpy(O.pack(A, V)).cuda()
+    b1 = torch.from_numpy(O.pack(B, V, pad_diag=0.0)).cuda()
+    t1 = torch.zeros(ng * V * n, dtype=torch.float64, device="cuda")
+    it1 = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    be1 = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+    assert cbk_gb300.dgels_refined_compact("C", "N", m, n, nrhs, a1, m, b1, m, t1, V, nm,
+                                           iters=it1, berr=be1) == 0
+    lda, ldb = m + 2, m + 3
+    sa, sb = lda * n + 7, ldb * nrhs + 1
+    a2 = torch.from_numpy(_dense(A, lda, sa, 5.0)).cuda()
+    b2 = torch.from_numpy(_dense(B, ldb, sb, 6.0)).cuda()
+    t2 = torch.zeros(nm * n, dtype=torch.float64, device="cuda")
+    it2 = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    be2 = torch.full((nm,), -1.0, dtype=torch.float64, device="cuda")
+    assert cbk_gb300.dgels_refined_batched("N", m, n, nrhs, a2, lda, sa, b2, ldb, sb, t2, nm,
+                                           iters=it2, berr=be2) == 0
+    torch.cuda.synchronize()
+    it = it1.cpu().numpy()
+    assert it[4] == -2 and np.array_equal(it2.cpu().numpy(), it)
+    assert np.array_equal(be2.cpu().numpy(), be1.cpu().numpy(), equal_nan=True)
+    bh, ah = b2.cpu().numpy(), a2.cpu().numpy()
+    assert np.array_equal(_undense(bh, nm, m, nrhs, ldb, sb),
+                          O.unpack(b1.cpu().numpy(), nm, m, nrhs, V))
+    Ad, Ac = _undense(ah, nm, m, n, lda, sa), O.unpack(a1.cpu().numpy(), nm, m, n, V)
+    assert np.array_equal(Ad, Ac)
+    T1 = t1.cpu().numpy().reshape(ng, n, V).transpose(0, 2, 1).reshape(-1, n)[:nm]
+    assert np.array_equal(t2.cpu().numpy().reshape(nm, n), T1)
+    assert (bh[_dense(np.zeros_like(B), ldb, sb, 1.0) == 1.0] == 6.0).all()
+    assert (ah[_dense(np.zeros_like(A), lda, sa, 1.0) == 1.0] == 5.0).all()
+    # n = 0: B := 0 inside each matrix, the padding kept
+    b3 = torch.from_numpy(_dense(B, ldb, sb, 6.0)).cuda()
+    assert cbk_gb300.dgels_refined_batched("N", m, 0, nrhs, a2, lda, sa, b3, ldb, sb, t2,
+                                           nm) == 0
+    torch.cuda.synchronize()
+    b3h = b3.cpu().numpy()
+    inside = _dense(np.zeros_like(B), ldb, sb, 1.0) == 0.0
+    assert (b3h[inside] == 0.0).all() and (b3h[~inside] == 6.0).all()
