@@ -31,6 +31,13 @@ cpu_baseline  the oracle (the C restatement of the reference's dposv_compact,
 With --gpus N > 1 (torchrun, one rank per GPU) every rank solves its own full
 replica of the workload: value = all ranks' solves / the slowest rank's time.
 --impl reference times the CPU implementation instead (rank 0 only).
+
+Other configurations print their own line (--config): c1 plain dposv n = 8 on
+65,536 matrices; c2 dgels 16 x 8 (nrhs 4) and dorgqr on 1,048,576; c4 the
+uneven-order dsysvnp in one CUDA-graph launch against one launch per order;
+c5 the mixed-precision least squares 64 x 16 (nrhs 8) against plain dgels;
+c3d the headline's refined solve on strided dense batches against the compact
+layout. --case KIND N NM runs one small solve for a profiler capture.
 """
 from __future__ import annotations
 
