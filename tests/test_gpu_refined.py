@@ -196,3 +196,29 @@ def test_refined_batched_equals_compact(n, nrhs, uplo, cuda):
     assert np.array_equal(Ad[5], Ac[5])
     ok = it >= 0
     assert np.array_equal(Ad[ok], A[ok])
+
+
+@pytest.mark.parametrize("n,nrhs,nm", [(1, 1, 5), (3, 3, 1), (64, 2, 9), (65, 1, 7), (17, 3, 33)])
+def test_refined_batched_edges(n, nrhs, nm, cuda):
+    """Dense batches at the edges: order 1, a single matrix, the last order of
+    the warp kernel (64) and the first of the workspace kernel (65), several
+    right-hand sides -- each matrix's x bit-identical to the compact path's."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(13 * n + nm)
+    A, _ = C.gen_spd_cond(rng, nm, n)
+    B = rng.standard_normal((nm, n, nrhs))
+    info, X, a1, a0, it, be = _run(A, B, 32, "C", "L")
+    assert info == 0
+    lda, ldb = n + 1, n + 2
+    sa, sb = lda * n + 3, ldb * nrhs
+    ad = torch.from_numpy(_dense(A, lda, sa, 0.0)).cuda()
+    bd = torch.from_numpy(_dense(B, ldb, sb, 0.0)).cuda()
+    itd = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    assert cbk_gb300.dposv_refined_batched("L", n, nrhs, ad, lda, sa, bd, ldb, sb, nm,
+                                           iters=itd) == 0
+    torch.cuda.synchronize()
+    bh = bd.cpu().numpy()
+    Xd = np.stack([bh[k * sb:k * sb + nrhs * ldb].reshape(nrhs, ldb)[:, :n].T for k in range(nm)])
+    assert np.array_equal(Xd, X) and np.array_equal(itd.cpu().numpy(), it)
