@@ -24,13 +24,15 @@ roofline   HBM roofline of the dominant launch (the largest order): algorithmic
            bytes (lower triangle of A read once, b read, x written) over its
            measured duration; fp64_pipe the same launch's FP64 work over the
            measured FP64 FMA rate -- the pipe that binds on this part
-cpu_baseline  the oracle (the C restatement of the reference's dposv_compact,
-           -O3, OpenMP over groups of V = 8, every host core) on a bounded
-           sample of the same workload
+cpu_baseline  the reference's own dposv_compact (its src/cbk.cpp built -O3 for
+           the host's native vector ISA, OpenMP over groups, every host core)
+           on this run's matrices copied to the host, at the fastest of the
+           reference's widths 2/4/8
 
 With --gpus N > 1 (torchrun, one rank per GPU) every rank solves its own full
 replica of the workload: value = all ranks' solves / the slowest rank's time.
---impl reference times the CPU implementation instead (rank 0 only).
+--impl reference times the reference's own CPU build on the same workload
+instead (rank 0 only; the port of it where the reference could not be built).
 
 Other configurations print their own line (--config): c1 plain dposv n = 8 on
 65,536 matrices; c2 dgels 16 x 8 (nrhs 4) and dorgqr on 1,048,576; c4 the
@@ -61,7 +63,6 @@ V = 32
 NRHS = 1
 SEED = 0x5EED
 LOG10_KAPPA = (1.0, 6.0)
-CPU_SAMPLE = 16384  # matrices per order in the CPU timing sample
 WORKLOAD = ("mixed-precision dposv_compact: n in {8,16,32,48}, nrhs=1, 262144 SPD matrices "
             "per n (kappa log-uniform 1e1..1e6), compact V=32 column-major lower")
 DATA = ("synthetic (seed 0x5EED): A = U diag(s) U^T, U Haar (sign-fixed QR of a Gaussian), "
@@ -166,66 +167,196 @@ class Clocks:
 # CPU implementation (the reference arm, and the cpu_baseline of ours)
 # ---------------------------------------------------------------------------
 
-def cpu_sample(seed=SEED, per_n=CPU_SAMPLE):
+CPU_WIDTHS = (2, 4, 8)  # the reference's widths: NEON holds 2 doubles, AVX-512 8
+
+
+def cpu_lib():
+    """(library, kind): the reference's own src/cbk.cpp in its performance build
+    (oracle/_ref/libcbk_ref_fast.so: -O3, the host's native vector ISA,
+    OpenMP), or, where the reference could not be built, the oracle's port."""
+    from oracle import oracle as O
+    lib = O.reference(fast=True)
+    if lib is not None:
+        return lib, "reference"
+    return O.oracle(fast=True), "port"
+
+
+def cpu_threads():
+    """OpenMP threads a parallel region of the CPU library gets."""
+    import ctypes
+    try:
+        gomp = ctypes.CDLL("libgomp.so.1")
+        gomp.omp_get_max_threads.restype = ctypes.c_int
+        return int(gomp.omp_get_max_threads())
+    except OSError:
+        return os.cpu_count()
+
+
+def cpu_info():
+    import platform
+    info = {"machine": platform.machine(), "logical_cpus": os.cpu_count(),
+            "omp_threads": cpu_threads()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                info["model"] = ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
+
+
+def cpu_pass(lib, packed, Vc, nm):
+    """One step over `packed` [(n, a, b)] with the library's dposv_compact at
+    width Vc; the inputs are restored from the pristine arrays untimed before
+    each call (the reference benches' method). Returns seconds per order."""
+    import numpy as np
+    out = []
+    for n, a0, b0, a, b in packed:
+        np.copyto(a, a0)
+        np.copyto(b, b0)
+        t0 = time.perf_counter()
+        info = lib.call("posv", np.float64, "C", "L", n, NRHS, a, n, b, n, Vc, nm)
+        out.append(time.perf_counter() - t0)
+        assert info == 0, info
+    return out
+
+
+def cpu_packed(dense, Vc):
+    """[(n, A, B)] dense -> [(n, a0, b0, a, b)] compact at width Vc (pristine
+    and working copies)."""
+    from oracle import oracle as O
+    out = []
+    for n, A, B in dense:
+        a0, b0 = O.pack(A, Vc), O.pack(B, Vc, pad_diag=0.0)
+        out.append((n, a0, b0, a0.copy(), b0.copy()))
+    return out
+
+
+def cpu_pick_width(lib, dense, nm, reps=2):
+    """The fastest of the reference's widths on `dense` (best of reps passes
+    each); returns (V, {V: ms per pass})."""
+    times = {}
+    for Vc in CPU_WIDTHS:
+        packed = cpu_packed(dense, Vc)
+        cpu_pass(lib, packed, Vc, nm)
+        times[Vc] = 1e3 * min(sum(cpu_pass(lib, packed, Vc, nm)) for _ in range(reps))
+        del packed
+    return min(times, key=times.get), times
+
+
+def _gen_chunk(task):
+    """A chunk of the headline workload for one order, packed at width Vc
+    (a spawned worker of the reference arm's input generation)."""
+    n, count, seed, Vc = task
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import cases as C
     from oracle import oracle as O
     rng = np.random.default_rng(seed)
-    data = []
-    for n in SIZES:
-        A, _ = C.gen_spd_cond(rng, per_n, n, LOG10_KAPPA)
-        B = rng.standard_normal((per_n, n, NRHS))
-        data.append((n, O.pack(A, 8), O.pack(B, 8, pad_diag=0.0)))
-    return data
+    A, _ = C.gen_spd_cond(rng, count, n, LOG10_KAPPA)
+    B = rng.standard_normal((count, n, NRHS))
+    return O.pack(A, Vc), O.pack(B, Vc, pad_diag=0.0)
 
 
-def cpu_time_step(lib, data):
-    """One pass over the sample with the reference's dposv_compact (V = 8,
-    the AVX-512 / two-NEON-register double width); returns seconds."""
+def cpu_workload(Vc, per_n=NM, chunk=16384):
+    """The full headline workload on the host, packed at width Vc: for every
+    order per_n matrices from the same distribution as the GPU arm's, made by
+    a pool of spawned single-threaded workers (one seeded chunk each).
+    Returns [(n, a0, b0, a, b)]."""
+    import multiprocessing as mp
+
     import numpy as np
-    work = [(n, a.copy(), b.copy()) for n, a, b in data]
-    t0 = time.perf_counter()
-    for n, a, b in work:
-        info = lib.call("posv", np.float64, "C", "L", n, NRHS, a, n, b, n, 8, CPU_SAMPLE)
-        assert info == 0
-    return time.perf_counter() - t0
+    seeds = np.random.SeedSequence(SEED).spawn(len(SIZES) * (per_n // chunk))
+    tasks = [(n, chunk, seeds[k * (per_n // chunk) + c], Vc)
+             for k, n in enumerate(SIZES) for c in range(per_n // chunk)]
+    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")}
+    os.environ.update(OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    try:
+        pool = mp.get_context("spawn").Pool(processes=max(1, min(32, os.cpu_count() or 1)))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    with pool:
+        parts = pool.map(_gen_chunk, tasks, chunksize=1)
+    out = []
+    per = per_n // chunk
+    for k, n in enumerate(SIZES):
+        a0 = np.concatenate([parts[k * per + c][0] for c in range(per)])
+        b0 = np.concatenate([parts[k * per + c][1] for c in range(per)])
+        out.append((n, a0, b0, a0.copy(), b0.copy()))
+    return out
 
 
-def cpu_baseline(steps=3):
-    from oracle import oracle as O
-    lib = O.oracle(fast=True)
-    data = cpu_sample()
-    cpu_time_step(lib, data)  # warm-up
-    best = min(cpu_time_step(lib, data) for _ in range(steps))
-    solves = CPU_SAMPLE * len(SIZES)
-    return {"value": solves / best, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-            "sample": (f"{CPU_SAMPLE} matrices per n in {{8,16,32,48}} from the same "
-                       f"distribution, dposv_compact V=8, best of {steps} passes "
-                       f"({best * 1e3:.1f} ms per pass)")}
+def cpu_baseline_from(dense_fn, steps=3):
+    """cpu_baseline of our arm: the reference's dposv_compact (its performance
+    build) on the GPU run's own matrices, copied to the host, at the fastest
+    of its widths; best of `steps` passes. dense_fn() gives [(n, A, B)]."""
+    lib, kind = cpu_lib()
+    dense = dense_fn()
+    nm = dense[0][1].shape[0]
+    Vc, wtimes = cpu_pick_width(lib, [(n, A[:16384], B[:16384]) for n, A, B in dense], 16384)
+    packed = cpu_packed(dense, Vc)
+    del dense
+    cpu_pass(lib, packed, Vc, nm)  # warm-up
+    best = min(sum(cpu_pass(lib, packed, Vc, nm)) for _ in range(steps))
+    return {"value": nm * len(SIZES) / best, "unit": UNIT, "cores": cpu_threads(), "kind": kind,
+            "V": Vc, "width_ms_16384_per_n": wtimes, "host": cpu_info(),
+            "sample": (f"the GPU run's own matrices, all {nm} per n in {{8,16,32,48}}, "
+                       f"dposv_compact at V={Vc} (fastest of {CPU_WIDTHS} on 16384 per n), "
+                       f"best of {steps} passes ({best * 1e3:.1f} ms per pass)")}
 
 
 def run_reference(args):
+    """--impl reference: the reference's own CPU implementation (its
+    performance build) on the same workload and config as the GPU arm, rank 0
+    alone; the other ranks exit without work."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return
-    from oracle import oracle as O
-    lib = O.oracle(fast=True)
-    data = cpu_sample()
+    import numpy as np
+    lib, kind = cpu_lib()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases as C
+    per_n = args.ref_per_n
+    nsub = min(16384, per_n)
+    rng = np.random.default_rng(SEED)
+    sub = []
+    for n in SIZES:
+        A, _ = C.gen_spd_cond(rng, nsub, n, LOG10_KAPPA)
+        sub.append((n, A, rng.standard_normal((nsub, n, NRHS))))
+    Vc, wtimes = cpu_pick_width(lib, sub, nsub)
+    wtimes = {f"{v} ({nsub} per n)": t for v, t in wtimes.items()}
+    del sub
+    t0 = time.perf_counter()
+    packed = cpu_workload(Vc, per_n, chunk=nsub)
+    gen_s = time.perf_counter() - t0
     for _ in range(args.warmup):
-        cpu_time_step(lib, data)
-    times = [cpu_time_step(lib, data) for _ in range(args.steps)]
-    solves = CPU_SAMPLE * len(SIZES)
-    value = solves * args.steps / sum(times)
+        cpu_pass(lib, packed, Vc, per_n)
+    per = [cpu_pass(lib, packed, Vc, per_n) for _ in range(args.steps)]
+    tot = [sum(p) for p in per]
+    solves = per_n * len(SIZES)
+    ms = 1e3 * sum(tot) / len(tot)
+    value = solves / (ms * 1e-3)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": {"workload": WORKLOAD, "sample_per_n": CPU_SAMPLE, "V": 8,
-                   "threads": O.max_threads()},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-                         "sample": f"{CPU_SAMPLE} matrices per n, every step"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "nm_per_n": per_n, "n": list(SIZES), "nrhs": NRHS,
+                   "V": Vc, "parallelism": "OpenMP over groups of V (the reference's own)"},
+        "per_n_ms": {str(n): 1e3 * statistics.mean(p[k] for p in per)
+                     for k, n in enumerate(SIZES)},
+        "best_ms_per_step": 1e3 * min(tot),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": kind,
+                         "V": Vc, "width_ms": wtimes, "host": cpu_info(),
+                         "sample": (f"the whole workload every step: {per_n} matrices per n, "
+                                    f"dposv_compact at V={Vc} (fastest of {CPU_WIDTHS}); "
+                                    f"inputs made by a spawned pool in {gen_s:.0f} s, "
+                                    f"restored untimed before every call")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -579,7 +710,8 @@ def run_gpu(args):
         "clocks": clocks,
     }
     if ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline_from(
+            lambda: [(b["n"], b["A"].cpu().numpy(), b["B"].cpu().numpy()) for b in batches])
     if not args.no_e2e:
         line["e2e"] = e2e(args, cbk, batches, barrier, ws)
     # free the device before printing
@@ -876,6 +1008,8 @@ def main():
                     help="keep the built-in launch shapes instead of autotuning them first")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-per-n", type=int, default=NM,
+                    help="--impl reference: matrices per order (default: the whole workload)")
     ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5", "c3d"), default="c3",
                     help="c3 (default) is the headline; the others print their own line")
     ap.add_argument("--case", nargs=3, metavar=("KIND", "N", "NM"),

@@ -104,14 +104,17 @@ def oracle(fast: bool = False) -> CbkLib:
     return _LIBS[name]
 
 
-def reference() -> CbkLib | None:
-    """The reference's own build, or None where it was not built."""
-    path = os.path.join(HERE, "_ref", "libcbk_ref.so")
+def reference(fast: bool = False) -> CbkLib | None:
+    """The reference's own build, or None where it was not built: the pin
+    build (no contraction) or, fast=True, its performance build (-O3, the
+    host's native vector ISA, OpenMP), the timed CPU baseline."""
+    name = "libcbk_ref_fast.so" if fast else "libcbk_ref.so"
+    path = os.path.join(HERE, "_ref", name)
     if not os.path.exists(path):
         return None
-    if "ref" not in _LIBS:
-        _LIBS["ref"] = CbkLib(path, "")
-    return _LIBS["ref"]
+    if name not in _LIBS:
+        _LIBS[name] = CbkLib(path, "")
+    return _LIBS[name]
 
 
 def max_threads() -> int:

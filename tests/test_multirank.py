@@ -66,7 +66,8 @@ def test_single_process_needs_no_collective():
 def test_reference_arm_under_torchrun_prints_once(oracle_lib):
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3",
+           "--ref-per-n", "1024"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
                        env=dict(os.environ, OMP_NUM_THREADS="2"))
     assert r.returncode == 0, r.stderr[-2000:]
