@@ -380,6 +380,9 @@ const char *cbk_cuda_status_string(int info)
     if (info < 0) return "illegal argument (the -info-th)";
     if (info >= CBK_CUDA_ERROR_BASE)
         return cudaGetErrorString((cudaError_t)(info - CBK_CUDA_ERROR_BASE));
+    if (info == CBK_CUDA_NOALLOC_TOO_LARGE) return "batch too large for the no-allocation scratch";
+    if (info == CBK_CUDA_NOALLOC_IN_CAPTURE)
+        return "first no-allocation call in this CUDA context made on a capturing stream";
     return "unknown status";
 }
 
@@ -593,9 +596,10 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
     if (int e = sym_solve_args(layout, uplo, n, nrhs, ldap, ldbp, V, nm, row, up)) return e;
     if (max_iter < 0) return -11;
     if (n == 0 || nm == 0 || nrhs == 0) return 0;
-    if (posv_refined_lwork(n, nrhs, V, nm) > (size_t)CBK_CUDA_NOALLOC_SCRATCH_BYTES) return -10;
-    return cuda_status(launch_posv_refined_noalloc(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
-                                                   max_iter, iters, berr, S(st)));
+    if (posv_refined_lwork(n, nrhs, V, nm) > (size_t)CBK_CUDA_NOALLOC_SCRATCH_BYTES)
+        return CBK_CUDA_NOALLOC_TOO_LARGE;
+    return launch_posv_refined_noalloc(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter,
+                                       iters, berr, S(st));
 }
 
 long long cbk_cuda_dgels_refined_compact_lwork(int m, int n, int nrhs, int V, int nm)

@@ -37,7 +37,7 @@
 
 #include "../../include/cbk_cuda.h"
 
-#include <atomic>
+#include <mutex>
 #include <float.h>
 #include <math.h>
 
@@ -476,10 +476,16 @@ cudaError_t launch_count_negative(const int *iters, int n, int *count, cudaStrea
 // cbk_cuda_dposv_refined_compact_noalloc_async takes no workspace: for
 // n > 64 the FP32 factor, x and the correction live in this one array,
 // reserved on every GPU that loads the library for as long as the process
-// runs. Host code cannot use the array's name as a device address, so the
-// address is looked up once per device, with that device current, and passed
-// to the kernel. Every call shares the array and nothing in it needs to start
-// at zero: the kernel writes each element it reads (the FP32 copy of A before
+// runs. Host code cannot use the array's name as a device address: the
+// address belongs to the CUDA context the module is loaded in, so it is
+// looked up (cudaGetSymbolAddress, which allocates nothing) with that context
+// current and cached under the context's unique ID -- a context made later
+// on the same device (a driver-API host's own, or the primary context again
+// after cudaDeviceReset) has a new ID and gets its own lookup. A lookup is
+// refused on a capturing stream (it may load the module, which a capture
+// does not allow): the first call in each context must come before any
+// capture. Every call shares the array and nothing in it needs to start at
+// zero: the kernel writes each element it reads (the FP32 copy of A before
 // the factorization, x and the correction before each use).
 
 namespace {
@@ -487,22 +493,85 @@ namespace {
 static_assert(CBK_CUDA_NOALLOC_SCRATCH_BYTES % 256 == 0, "scratch size");
 __device__ __align__(256) unsigned char g_noalloc_scratch[CBK_CUDA_NOALLOC_SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::atomic<void *> g_noalloc_addr[MAX_DEVICES];
+// the driver's cuCtxGetCurrent and cuCtxGetId, resolved through the runtime
+// (no link-time dependence on libcuda)
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
 
-// The device address of the scratch array on the current device (looked up on
-// the first call per device, which should come before any stream capture).
-cudaError_t noalloc_scratch(void **out)
+struct CtxFns {
+    CtxGetCurrentFn current = nullptr;
+    CtxGetIdFn id = nullptr;
+};
+
+const CtxFns &ctx_fns()
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
+    static const CtxFns f = [] {
+        CtxFns r;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            r.current = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            r.id = reinterpret_cast<CtxGetIdFn>(p);
+        return r;
+    }();
+    return f;
+}
+
+// the unique ID of the current context; false when none is current
+bool current_ctx_id(unsigned long long &id)
+{
+    const CtxFns &f = ctx_fns();
+    void *ctx = nullptr;
+    return f.current && f.id && f.current(&ctx) == 0 && ctx != nullptr && f.id(ctx, &id) == 0;
+}
+
+constexpr int CACHE = 64;
+struct Slot {
+    unsigned long long ctx;
+    void *addr;
+};
+std::mutex g_cache_mu;
+Slot g_cache[CACHE];
+int g_cache_n = 0, g_cache_next = 0;
+
+// The scratch array's address in the current context. On a capturing stream
+// only a cached address is used: *capturing is set, and nothing looked up,
+// when there is none.
+cudaError_t noalloc_scratch(cudaStream_t s, void **out, bool *capturing)
+{
+    *capturing = false;
+    unsigned long long id = 0;
+    bool have = current_ctx_id(id);
+    if (have) {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (int k = 0; k < g_cache_n; ++k)
+            if (g_cache[k].ctx == id) {
+                *out = g_cache[k].addr;
+                return cudaSuccess;
+            }
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cs);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
-    void *p = g_noalloc_addr[dev].load(std::memory_order_acquire);
-    if (p == nullptr) {
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_addr[dev].store(p, std::memory_order_release);
+    if (cs != cudaStreamCaptureStatusNone) {
+        *capturing = true;
+        return cudaSuccess;
+    }
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    if (!have) have = current_ctx_id(id); // the lookup made the primary context current
+    if (have) {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        g_cache[g_cache_next] = Slot{id, p};
+        g_cache_next = (g_cache_next + 1) % CACHE;
+        g_cache_n = g_cache_n < CACHE ? g_cache_n + 1 : CACHE;
     }
     *out = p;
     return cudaSuccess;
@@ -510,17 +579,20 @@ cudaError_t noalloc_scratch(void **out)
 
 } // namespace
 
-cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
-                                        double *bp, int ldbp, int V, int nm, int max_iter,
-                                        int *iters, double *berr, cudaStream_t s)
+int launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
+                                double *berr, cudaStream_t s)
 {
     void *work = nullptr;
     if (posv_refined_lwork(n, nrhs, V, nm) > 0) {
-        const cudaError_t e = noalloc_scratch(&work);
-        if (e != cudaSuccess) return e;
+        bool capturing = false;
+        const cudaError_t e = noalloc_scratch(s, &work, &capturing);
+        if (e != cudaSuccess) return CBK_CUDA_ERROR_BASE + (int)e;
+        if (capturing) return CBK_CUDA_NOALLOC_IN_CAPTURE;
     }
-    return launch_posv_refined(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, max_iter, iters, berr,
-                               work, s);
+    const cudaError_t e = launch_posv_refined(row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
+                                              max_iter, iters, berr, work, s);
+    return e == cudaSuccess ? 0 : CBK_CUDA_ERROR_BASE + (int)e;
 }
 
 } // namespace cbkcuda

@@ -136,9 +136,11 @@ cudaError_t launch_tri_copy(bool row, bool up, int n, int ld, int V, long groups
 // *count += the number of negative entries of iters[0 .. n)
 cudaError_t launch_count_negative(const int *iters, int n, int *count, cudaStream_t s);
 
-// the same with the library's own scratch array (no allocation, no workspace)
-cudaError_t launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
-                                        double *bp, int ldbp, int V, int nm, int max_iter,
-                                        int *iters, double *berr, cudaStream_t s);
+// the same with the library's own scratch array (no allocation, no
+// workspace); returns 0, CBK_CUDA_NOALLOC_IN_CAPTURE or CBK_CUDA_ERROR_BASE +
+// a CUDA error
+int launch_posv_refined_noalloc(bool row, bool up, int n, int nrhs, double *ap, int ldap,
+                                double *bp, int ldbp, int V, int nm, int max_iter, int *iters,
+                                double *berr, cudaStream_t s);
 
 } // namespace cbkcuda

@@ -412,18 +412,25 @@ int cbk_cuda_graph_destroy(cbk_cuda_graph graph);
  * on every GPU it is used on, for as long as the process runs. n <= 64 needs
  * none.
  * Arguments, results and return codes are those of
- * cbk_cuda_dposv_refined_compact_async without work and lwork, plus -10 when
- * the batch is too large for the array: when
- * cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) exceeds
- * CBK_CUDA_NOALLOC_SCRATCH_BYTES (for n = 80, about 2,500 matrices; split
- * larger batches into several calls).
- * The first call on a device looks up the array's device address with that
- * device current: make that first call before any stream capture. Every call
- * shares the one array, and it keeps the last call's contents; nothing in it
- * needs to start at zero. Calls that overlap on the GPU -- on different
- * streams, or from host threads without ordering between them -- race on the
- * array and give wrong results: serialise them on one stream. */
+ * cbk_cuda_dposv_refined_compact_async without work and lwork, plus:
+ *   CBK_CUDA_NOALLOC_TOO_LARGE  the batch does not fit the array:
+ *          cbk_cuda_dposv_refined_compact_lwork(n, nrhs, V, nm) exceeds
+ *          CBK_CUDA_NOALLOC_SCRATCH_BYTES (for n = 80, about 2,500 matrices;
+ *          split larger batches into several calls); checked after the
+ *          argument codes, before any device work
+ *   CBK_CUDA_NOALLOC_IN_CAPTURE  the first n > 64 call in this CUDA context
+ *          came on a capturing stream: nothing was enqueued
+ * The first n > 64 call in each CUDA context (each device's primary context,
+ * a driver-API context of the caller's, the primary context again after a
+ * cudaDeviceReset) looks up the array's address in that context: make it
+ * before any stream capture. Every call shares the one array, and it keeps
+ * the last call's contents; nothing in it needs to start at zero. Calls that
+ * overlap on the GPU -- on different streams, or from host threads without
+ * ordering between them -- race on the array and give wrong results:
+ * serialise them on one stream. */
 #define CBK_CUDA_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define CBK_CUDA_NOALLOC_TOO_LARGE 900
+#define CBK_CUDA_NOALLOC_IN_CAPTURE 901
 int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, int nrhs,
                                                  double *ap, int ldap, double *bp, int ldbp,
                                                  int V, int nm, int max_iter, int *iters,

@@ -201,3 +201,44 @@ def test_refined_gels_batched_argument_checks():
     assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -17
     assert f("N", 8, 4, 0, None, 8, 32, None, 8, 8, None, 10) == 0
     assert cbk_gb300.dgels_refined_batched_lwork(-1, 1, 1, 1) == -1
+
+
+def _noalloc_fn():
+    import ctypes
+
+    import cbk_gb300
+    f = cbk_gb300.lib().cbk_cuda_dposv_refined_compact_noalloc_async
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    return f
+
+
+def test_noalloc_entry_validates_before_any_device_work():
+    """The no-allocation refined solve: the argument codes of the workspace
+    entry point, the quick returns, and CBK_CUDA_NOALLOC_TOO_LARGE (900) --
+    distinct from -10, an illegal nm -- for a batch beyond the 64 MiB array;
+    all before any device work (here: no GPU at all, null pointers)."""
+    import cbk_gb300
+    f = _noalloc_fn()
+    scratch = 64 << 20  # CBK_CUDA_NOALLOC_SCRATCH_BYTES
+    n, V = 80, 32
+    lw = cbk_gb300.dposv_refined_lwork
+    fits = max(nm for nm in range(32, 20000, 32) if lw(n, 1, V, nm) <= scratch)
+    assert lw(n, 1, V, fits + 32) > scratch
+    assert f(b"X", b"L", n, 1, None, n, None, n, V, 64, 10, None, None, None) == -1
+    assert f(b"C", b"Q", n, 1, None, n, None, n, V, 64, 10, None, None, None) == -2
+    assert f(b"C", b"L", -1, 1, None, n, None, n, V, 64, 10, None, None, None) == -3
+    assert f(b"C", b"L", n, -1, None, n, None, n, V, 64, 10, None, None, None) == -4
+    assert f(b"C", b"L", n, 1, None, n - 1, None, n, V, 64, 10, None, None, None) == -6
+    assert f(b"C", b"L", n, 1, None, n, None, n - 1, V, 64, 10, None, None, None) == -8
+    assert f(b"C", b"L", n, 1, None, n, None, n, 33, 64, 10, None, None, None) == -9
+    assert f(b"C", b"L", n, 1, None, n, None, n, V, -1, 10, None, None, None) == -10
+    assert f(b"C", b"L", n, 1, None, n, None, n, V, 64, -1, None, None, None) == -11
+    assert f(b"C", b"L", n, 1, None, n, None, n, V, fits + 32, 10, None, None, None) == 900
+    assert f(b"C", b"L", n, 1, None, n, None, n, V, 0, 10, None, None, None) == 0
+    assert f(b"C", b"L", n, 0, None, n, None, n, V, 10 ** 6, 10, None, None, None) == 0
+    assert f(b"C", b"L", 0, 1, None, 1, None, 1, V, 10 ** 6, 10, None, None, None) == 0
+    assert "too large" in cbk_gb300.status_string(900)
+    assert "capturing" in cbk_gb300.status_string(901)
