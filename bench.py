@@ -75,6 +75,12 @@ def bytes_per_matrix(n: int) -> int:
     return 8 * (n * (n + 1) // 2 + 2 * n * NRHS)
 
 
+def plain_bytes_per_matrix(n: int, nrhs: int = NRHS) -> int:
+    """Algorithmic HBM bytes of one plain FP64 dposv: the lower triangle of A
+    read once and its factor written back, b read and x written."""
+    return 8 * (2 * (n * (n + 1) // 2) + 2 * n * nrhs)
+
+
 def plain_flops(n: int) -> float:
     """FP64 flops of the plain factor + solve: n^3/3 + n^2/2 + n/6 + 2 n^2 nrhs."""
     return n ** 3 / 3 + n * n / 2 + n / 6 + 2 * n * n * NRHS
@@ -849,7 +855,7 @@ def run_config(args):
                     unit=UNIT, ms_per_step=t, dtype="f64",
                     data="synthetic: A = G G^T + n I, G, B ~ N(0,1), seed 0x5EED",
                     max_berr_over_n_eps=berr, refined_value=nm / (tr * 1e-3),
-                    gbs=nm * bytes_per_matrix(n) * 704 / 416 / (t * 1e-3) / 1e9,
+                    gbs=nm * plain_bytes_per_matrix(n, 1) / (t * 1e-3) / 1e9,
                     gpu_launches=args.steps)
         line["config"]["workload"] = "dposv_compact n=8 nrhs=1, 65536 matrices, V=32"
     elif args.config == "c2":

@@ -2,7 +2,7 @@
 // in and out pipelined with the solves.
 //
 // The reference's calling convention keeps every array in host memory
-// (include/cbk.h:218-234, its MKL-style adapter src/cbk_compat.cpp copies
+// (include/cbk.h:196-212, its MKL-style adapter src/cbk_compat.cpp copies
 // nothing because its kernels run on the CPU). Here a host batch is cut into
 // chunks of whole groups that flow through NBUF device slots, each slot on its
 // own stream: while one chunk is solved, the next one is copied in and the

@@ -51,7 +51,7 @@ extern "C" {
 /* Same type as cudaStream_t; 0 is the legacy default stream. */
 typedef struct CUstream_st *cbk_stream_t;
 
-/* Replaces cbk_get_version (include/cbk.h:77, src/cbk.cpp:36-39): the version
+/* Replaces cbk_get_version (include/cbk.h:76-77, src/cbk.cpp:36-39): the version
  * of the API implemented, encoded as CBK_VERSION is (0.2.0 -> 200). */
 int cbk_cuda_get_version(void);
 
@@ -64,7 +64,7 @@ const char *cbk_cuda_status_string(int info);
 /* The declarations below come in pairs per scalar type (d = double,
  * s = float): NAME(...) on stream 0 and NAME_async(..., stream). */
 
-/* QR factorization (include/cbk.h:96-113). -1 layout -2 m -3 n -5 ldap -7 V -8 nm */
+/* QR factorization (include/cbk.h:79-95). -1 layout -2 m -3 n -5 ldap -7 V -8 nm */
 int cbk_cuda_dgeqrf_compact(char layout, int m, int n, double *ap, int ldap, double *taup,
                             int V, int nm);
 int cbk_cuda_dgeqrf_compact_async(char layout, int m, int n, double *ap, int ldap,
@@ -74,7 +74,7 @@ int cbk_cuda_sgeqrf_compact(char layout, int m, int n, float *ap, int ldap, floa
 int cbk_cuda_sgeqrf_compact_async(char layout, int m, int n, float *ap, int ldap, float *taup,
                                   int V, int nm, cbk_stream_t stream);
 
-/* Apply Q or Q^T from either side (include/cbk.h:115-143).
+/* Apply Q or Q^T from either side (include/cbk.h:97-123).
  * -1 layout -2 side -3 trans -4 m -5 n -6 k -8 ldap -11 ldcp -12 V -13 nm */
 int cbk_cuda_dormqr_compact(char layout, char side, char trans, int m, int n, int k,
                             const double *ap, int ldap, const double *taup, double *cp,
@@ -89,7 +89,7 @@ int cbk_cuda_sormqr_compact_async(char layout, char side, char trans, int m, int
                                   const float *ap, int ldap, const float *taup, float *cp,
                                   int ldcp, int V, int nm, cbk_stream_t stream);
 
-/* Form the explicit Q in place (include/cbk.h:145-168).
+/* Form the explicit Q in place (include/cbk.h:125-150).
  * -1 layout -2 m -3 n -4 k -6 ldap -8 V -9 nm; k = 0 writes I(:, 0:n-1) */
 int cbk_cuda_dorgqr_compact(char layout, int m, int n, int k, double *ap, int ldap,
                             const double *taup, int V, int nm);
@@ -100,7 +100,7 @@ int cbk_cuda_sorgqr_compact(char layout, int m, int n, int k, float *ap, int lda
 int cbk_cuda_sorgqr_compact_async(char layout, int m, int n, int k, float *ap, int ldap,
                                   const float *taup, int V, int nm, cbk_stream_t stream);
 
-/* Cholesky factorization (include/cbk.h:170-189). -1 layout -2 uplo -3 n
+/* Cholesky factorization (include/cbk.h:151-170). -1 layout -2 uplo -3 n
  * -5 ldap -6 V -7 nm; the strictly-opposite triangle is never touched */
 int cbk_cuda_dpotrf_compact(char layout, char uplo, int n, double *ap, int ldap, int V,
                             int nm);
@@ -110,7 +110,7 @@ int cbk_cuda_spotrf_compact(char layout, char uplo, int n, float *ap, int ldap, 
 int cbk_cuda_spotrf_compact_async(char layout, char uplo, int n, float *ap, int ldap, int V,
                                   int nm, cbk_stream_t stream);
 
-/* Solve from a Cholesky factor (include/cbk.h:191-216). -1 layout -2 uplo -3 n
+/* Solve from a Cholesky factor (include/cbk.h:171-195). -1 layout -2 uplo -3 n
  * -4 nrhs -6 ldap -8 ldbp -9 V -10 nm */
 int cbk_cuda_dpotrs_compact(char layout, char uplo, int n, int nrhs, const double *ap,
                             int ldap, double *bp, int ldbp, int V, int nm);
@@ -123,7 +123,7 @@ int cbk_cuda_spotrs_compact_async(char layout, char uplo, int n, int nrhs, const
                                   int ldap, float *bp, int ldbp, int V, int nm,
                                   cbk_stream_t stream);
 
-/* Fused Cholesky factor + solve (include/cbk.h:218-234): bit-identical to
+/* Fused Cholesky factor + solve (include/cbk.h:196-212): bit-identical to
  * ?potrf then ?potrs; nrhs = 0 still factors. Codes as ?potrs. */
 int cbk_cuda_dposv_compact(char layout, char uplo, int n, int nrhs, double *ap, int ldap,
                            double *bp, int ldbp, int V, int nm);
@@ -134,7 +134,7 @@ int cbk_cuda_sposv_compact(char layout, char uplo, int n, int nrhs, float *ap, i
 int cbk_cuda_sposv_compact_async(char layout, char uplo, int n, int nrhs, float *ap, int ldap,
                                  float *bp, int ldbp, int V, int nm, cbk_stream_t stream);
 
-/* Unpivoted LDL^T factorization (include/cbk.h:236-258). Codes as ?potrf. */
+/* Unpivoted LDL^T factorization (include/cbk.h:213-238). Codes as ?potrf. */
 int cbk_cuda_dsytrfnp_compact(char layout, char uplo, int n, double *ap, int ldap, int V,
                               int nm);
 int cbk_cuda_dsytrfnp_compact_async(char layout, char uplo, int n, double *ap, int ldap, int V,
@@ -144,7 +144,7 @@ int cbk_cuda_ssytrfnp_compact(char layout, char uplo, int n, float *ap, int ldap
 int cbk_cuda_ssytrfnp_compact_async(char layout, char uplo, int n, float *ap, int ldap, int V,
                                     int nm, cbk_stream_t stream);
 
-/* Solve from an LDL^T factor (include/cbk.h:260-285). Codes as ?potrs. */
+/* Solve from an LDL^T factor (include/cbk.h:239-262). Codes as ?potrs. */
 int cbk_cuda_dsytrsnp_compact(char layout, char uplo, int n, int nrhs, const double *ap,
                               int ldap, double *bp, int ldbp, int V, int nm);
 int cbk_cuda_dsytrsnp_compact_async(char layout, char uplo, int n, int nrhs, const double *ap,
@@ -156,7 +156,7 @@ int cbk_cuda_ssytrsnp_compact_async(char layout, char uplo, int n, int nrhs, con
                                     int ldap, float *bp, int ldbp, int V, int nm,
                                     cbk_stream_t stream);
 
-/* Fused LDL^T factor + solve (include/cbk.h:287-303). Codes as ?potrs. */
+/* Fused LDL^T factor + solve (include/cbk.h:263-279). Codes as ?potrs. */
 int cbk_cuda_dsysvnp_compact(char layout, char uplo, int n, int nrhs, double *ap, int ldap,
                              double *bp, int ldbp, int V, int nm);
 int cbk_cuda_dsysvnp_compact_async(char layout, char uplo, int n, int nrhs, double *ap,
@@ -168,7 +168,7 @@ int cbk_cuda_ssysvnp_compact_async(char layout, char uplo, int n, int nrhs, floa
                                    int ldap, float *bp, int ldbp, int V, int nm,
                                    cbk_stream_t stream);
 
-/* Triangular solve (include/cbk.h:305-333). -1 layout -2 side -3 uplo
+/* Triangular solve (include/cbk.h:280-309). -1 layout -2 side -3 uplo
  * -4 transa -5 diag -6 m -7 n -10 ldap -12 ldbp -13 V -14 nm;
  * alpha = 0 sets B := 0 without reading A */
 int cbk_cuda_dtrsm_compact(char layout, char side, char uplo, char transa, char diag, int m,
@@ -184,7 +184,7 @@ int cbk_cuda_strsm_compact_async(char layout, char side, char uplo, char transa,
                                  int m, int n, float alpha, const float *ap, int ldap,
                                  float *bp, int ldbp, int V, int nm, cbk_stream_t stream);
 
-/* Least squares / minimum norm (include/cbk.h:335-351). -1 layout -2 trans
+/* Least squares / minimum norm (include/cbk.h:310-352). -1 layout -2 trans
  * -3 m -4 n -5 nrhs -7 ldap -9 ldbp -11 V -12 nm; min(m,n) = 0 sets B := 0,
  * nrhs = 0 does nothing */
 int cbk_cuda_dgels_compact(char layout, char trans, int m, int n, int nrhs, double *ap,
@@ -224,7 +224,7 @@ int cbk_cuda_sunpack_compact_async(char layout, int m, int n, const float *ap, i
 
 /* Mixed-precision SPD solve A X = B: FP32 Cholesky, FP64 iterative refinement
  * of each right-hand side, FP64 fallback per matrix. No reference entry
- * point: the ?posv_compact arguments (include/cbk.h:218-234) plus the method
+ * point: the ?posv_compact arguments (include/cbk.h:196-212) plus the method
  * of LAPACK dsposv. Per lane: x = solve32(b); r = b - A x in FP64 until
  * ||r||_inf <= sqrt(n) eps64 ||A||_inf ||x||_inf, correcting x += solve32(r);
  * a lane whose FP32 rounding overflows (iters = -2), whose FP32 pivot is not
@@ -273,7 +273,7 @@ int cbk_cuda_dposv_refined_batched_async(char uplo, int n, int nrhs, double *a, 
 /* The same solve on batches in HOST memory (ap, bp, iters, berr are host
  * pointers; pinned memory lets the copies overlap the solves). No reference
  * entry point: the reference's own calling convention -- every array on the
- * host, as in ?posv_compact (include/cbk.h:218-234) -- over the device solve
+ * host, as in ?posv_compact (include/cbk.h:196-212) -- over the device solve
  * above. The batch is cut into chunks of whole groups (about 48 MiB of
  * input each, at least 256 groups; the first and last a quarter of that)
  * that pass through three device slots on three streams, so that copying one
@@ -301,7 +301,7 @@ int cbk_cuda_dposv_refined_compact_host(char layout, char uplo, int n, int nrhs,
 /* Mixed-precision least squares min ||b - A x||, A m x n with m >= n: FP32
  * QR, FP64 refinement of the augmented system [I A; A^T 0][r; x] = [b; 0]
  * (Bjorck) per right-hand side, FP64 fallback per matrix. No reference entry
- * point: the ?gels_compact arguments (include/cbk.h:335-351) for the
+ * point: the ?gels_compact arguments (include/cbk.h:310-352) for the
  * overdetermined, non-transposed case. Per lane: x0 from the FP32 QR, then
  * f = b - r - A x and g = -A^T r in FP64, the correction from the FP32 QR,
  * until both residuals are at the FP64 rounding level of their terms

@@ -1,17 +1,19 @@
-/* The no-allocation refined solve in several CUDA contexts of one device,
- * and its refusal to make a first address lookup under stream capture.
+/* The no-allocation refined solve: its refusal to make a first address
+ * lookup under stream capture, and its results in more than one CUDA context
+ * of a device.
  *
  * A caller that cannot allocate may also own its CUDA contexts (a driver-API
  * host makes its own with cuCtxCreate). The library's scratch array has a
  * different address in each context, so each context's first n > 64 call
  * must look it up there. This program solves the same order-80 batch:
- *   1. in the device's primary context, through the workspace entry point and
- *      through cbk_cuda_dposv_refined_compact_noalloc_async (twice);
- *   2. in a second context of the same device, made current by cuCtxCreate,
- *      through the no-allocation entry point (twice);
- *   3. in a third context, first on a stream being captured -- the call must
- *      return CBK_CUDA_NOALLOC_IN_CAPTURE and enqueue nothing -- then outside
- *      the capture.
+ *   1. in the device's primary context, first on a stream being captured --
+ *      before any n > 64 call, so the call must return
+ *      CBK_CUDA_NOALLOC_IN_CAPTURE and enqueue nothing -- then outside it;
+ *   2. there again, through the workspace entry point (the reference result),
+ *      and once more through the no-allocation one;
+ *   3. in a second context of the same device made current by cuCtxCreate,
+ *      where the GPU allows one (a device in exclusive-process compute mode
+ *      does not: that step is then reported and skipped).
  * Every solution, iteration count and backward error must equal the
  * workspace entry point's bit for bit. The driver functions are resolved
  * through the runtime (no link-time libcuda). Exit code 0 and "noalloc ok"
@@ -133,8 +135,19 @@ int main(void)
     }
     int bad = 0;
     CK(cudaSetDevice(0));
+    {   /* initialise the library's runtime with a call that needs no scratch:
+         * one 1 x 1 system in a group of width 2, A = (4, pad 1), B = (2, 0) */
+        double *one;
+        CK(cudaMalloc((void **)&one, 4 * sizeof(double)));
+        const double h[4] = {4.0, 1.0, 2.0, 0.0};
+        CK(cudaMemcpy(one, h, sizeof h, cudaMemcpyHostToDevice));
+        if (cbk_cuda_dposv_compact('C', 'L', 1, 1, one, 1, one + 2, 1, 2, 1) != 0) bad = 1;
+        CK(cudaDeviceSynchronize());
+        CK(cudaFree(one));
+    }
+    bad |= solve(A, B, 1, 1, &got);
     bad |= solve(A, B, 0, 0, &ref);
-    bad |= solve(A, B, 1, 0, &got) || same("primary context", &ref, &got);
+    bad |= same("primary context, after a refused capture", &ref, &got);
     bad |= solve(A, B, 1, 0, &got) || same("primary context, second call", &ref, &got);
 
     ctx_create_fn create = NULL;
@@ -148,15 +161,17 @@ int main(void)
         printf("driver context functions unavailable\n");
         return 3;
     }
-    void *c2 = NULL, *c3 = NULL;
-    if (create(&c2, 0, 0) != 0) { printf("cuCtxCreate failed\n"); return 3; }
-    bad |= solve(A, B, 1, 0, &got) || same("second context", &ref, &got);
-    bad |= solve(A, B, 1, 0, &got) || same("second context, second call", &ref, &got);
-    if (create(&c3, 0, 0) != 0) { printf("cuCtxCreate failed\n"); return 3; }
-    bad |= solve(A, B, 1, 1, &got) || same("third context, after a refused capture", &ref, &got);
-    destroy(c3);
-    destroy(c2);
-    bad |= solve(A, B, 1, 0, &got) || same("primary context again", &ref, &got);
+    void *c2 = NULL;
+    const int rc = create(&c2, 0, 0);
+    if (rc != 0) {
+        printf("note: no second context on this device (cuCtxCreate %d): step 3 skipped\n", rc);
+    }
+    else {
+        bad |= solve(A, B, 1, 0, &got) || same("second context", &ref, &got);
+        bad |= solve(A, B, 1, 0, &got) || same("second context, second call", &ref, &got);
+        destroy(c2);
+        bad |= solve(A, B, 1, 0, &got) || same("primary context again", &ref, &got);
+    }
     if (bad) return 1;
     printf("noalloc ok\n");
     return 0;

@@ -290,6 +290,36 @@ def sweep(V_list=(2, 4, 8, 16), dtypes=(np.float64, np.float32), quick=False):
     return cases
 
 
+def benchmark_shapes(V=32, nm=37, dtypes=(np.float64, np.float32)):
+    """The orders and shapes the benchmark configurations run at, beyond the
+    sweep's orders (which stop at 33): the Cholesky solve at n = 32 and 48
+    with one right-hand side (the mixed-precision solve's FP64 comparator),
+    the LDL^T solve and both factorizations at n = 48, least squares at
+    64 x 16 with 8 right-hand sides and 16 x 8 with 4, and the thin Q at
+    16 x 8 -- both layouts and triangles, padded partial groups."""
+    out = []
+    seed = 9000
+    for dt in dtypes:
+        for lay, up in (("C", "L"), ("R", "U")):
+            for n in (32, 48):
+                seed += 1
+                out.append(make_case("posv", dt, seed, V, nm, lay, up, n, 1))
+            seed += 1
+            out.append(make_case("sysvnp", dt, seed, V, nm, lay, up, 48, 2))
+            seed += 1
+            out.append(make_case("potrf", dt, seed, V, nm, lay, up, 48))
+            seed += 1
+            out.append(make_case("sytrfnp", dt, seed, V, nm, lay, up, 48))
+        for lay in "CR":
+            seed += 1
+            out.append(make_case("gels", dt, seed, V, nm, lay, m=64, n=16, nrhs=8))
+            seed += 1
+            out.append(make_case("gels", dt, seed, V, nm, lay, m=16, n=8, nrhs=4))
+            seed += 1
+            out.append(make_case("orgqr", dt, seed, V, nm, lay, m=16, n=8, k=8))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # shapes of the array arguments, and re-interleaving a case at another width
 # ---------------------------------------------------------------------------

@@ -48,6 +48,10 @@ def select():
             count[c.routine] = k + 1
             if k % stride == 0:
                 picked.append(c)
+    # the benchmark configurations' orders and shapes (n = 32 / 48, 64 x 16),
+    # at the reference's width 2 with one padded lane: above the size cap, so
+    # kept to three matrices each
+    picked += C.benchmark_shapes(V=2, nm=3)
     return picked
 
 

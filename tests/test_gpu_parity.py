@@ -53,6 +53,21 @@ def test_parity_sweep(V, quick, cuda, oracle_lib):
     print(f"V={V}: {len(cases)} cases, worst ratio / order = {worst:.2f} eps")
 
 
+@pytest.mark.parametrize("V,nm", [(32, 37), (8, 11)])
+def test_parity_benchmark_shapes(V, nm, cuda, oracle_lib):
+    """The benchmark configurations' orders and shapes (plain FP64 and FP32
+    posv at n = 32 / 48, sysvnp and both factorizations at n = 48, gels at
+    64 x 16 with 8 right-hand sides and 16 x 8 with 4, orgqr 16 x 8) against
+    the oracle."""
+    worst = 0.0
+    cases = C.benchmark_shapes(V, nm)
+    for c in cases:
+        gi, g = G.run_gpu(c)
+        oi, o = C.run(oracle_lib, c)
+        worst = max(worst, _check(c, gi, g, oi, o))
+    print(f"benchmark shapes V={V}: {len(cases)} cases, worst ratio / order = {worst:.2f} eps")
+
+
 def test_parity_golden(cuda):
     worst = 0.0
     for cin, cout, info in make_golden.load():
@@ -80,7 +95,7 @@ def test_opposite_triangle_untouched(routine, layout, uplo, cuda):
 @pytest.mark.parametrize("layout,uplo", [("C", "L"), ("R", "U"), ("C", "U"), ("R", "L")])
 def test_fused_equals_separate(dtype, layout, uplo, cuda):
     """?posv == ?potrf then ?potrs and ?sysvnp == ?sytrfnp then ?sytrsnp, bit
-    for bit on the whole buffers (include/cbk.h:218-234, 287-303)."""
+    for bit on the whole buffers (include/cbk.h:196-212, 263-279)."""
     for n, nrhs in ((8, 1), (16, 3), (33, 5)):
         for fused, fac, sol in (("posv", "potrf", "potrs"), ("sysvnp", "sytrfnp", "sytrsnp")):
             c = C.make_case(fused, dtype, 7 * n + nrhs, 32, 70, layout, uplo, n, nrhs)

@@ -22,6 +22,15 @@ def test_oracle_reproduces_golden(oracle_lib):
     assert not bad, f"{len(bad)} fixtures differ, e.g. {bad[:5]}"
 
 
+def test_golden_pins_the_benchmark_orders():
+    """Orders above the sweep's 33 (the benchmark configurations' 48 and the
+    64 x 16 least squares) are among the reference-made fixtures."""
+    fx = make_golden.load()
+    assert any(c.routine == "posv" and c.kw["n"] == 48 for c, _, _ in fx)
+    assert any(c.routine == "sysvnp" and c.kw["n"] == 48 for c, _, _ in fx)
+    assert any(c.routine == "gels" and c.kw["m"] == 64 and c.kw["n"] == 16 for c, _, _ in fx)
+
+
 def test_golden_covers_every_routine():
     seen = {(c.routine, c.dtype) for c, _, _ in make_golden.load()}
     for r in C.ARGS:

@@ -9,9 +9,9 @@ the workspace entry point, so through the C ABI its solutions, iteration
 counts and backward errors must equal that entry point's bit for bit, twice
 in a row (the array keeps the previous call's contents, and nothing in it may
 leak into the next result); a warmed-up call must not change the device's
-free memory; and a C program checks the same in several CUDA contexts of one
-device and the refusal of a first address lookup under stream capture
-(tests/c/noalloc_check.c). Its argument codes are checked on the CPU in
+free memory; and a C program checks the refusal of a first address lookup
+under stream capture and, where the device allows a second CUDA context, the
+results in it (tests/c/noalloc_check.c). Its argument codes are checked on the CPU in
 tests/test_abi.py.
 """
 import ctypes
@@ -111,7 +111,7 @@ def test_noalloc_call_allocates_nothing(cuda):
     assert free1 == free0
 
 
-def test_noalloc_in_several_contexts_and_under_capture(tmp_path, cuda):
+def test_noalloc_refuses_lookup_under_capture_and_serves_contexts(tmp_path, cuda):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
