@@ -34,12 +34,16 @@ replica of the workload: value = all ranks' solves / the slowest rank's time.
 --impl reference times the reference's own CPU build on the same workload
 instead (rank 0 only; the port of it where the reference could not be built).
 
-Other configurations print their own line (--config): c1 plain dposv n = 8 on
+The other configurations are measured after the headline and reported in its
+line under "configs" (each with its own roofline and a cpu_baseline through
+the reference's own build on the same matrices): c1 plain dposv n = 8 on
 65,536 matrices; c2 dgels 16 x 8 (nrhs 4) and dorgqr on 1,048,576; c4 the
 uneven-order dsysvnp in one CUDA-graph launch against one launch per order;
-c5 the mixed-precision least squares 64 x 16 (nrhs 8) against plain dgels;
-c3d the headline's refined solve on strided dense batches against the compact
-layout. --case KIND N NM runs one small solve for a profiler capture.
+c5 the mixed-precision least squares 64 x 16 (nrhs 8) against plain dgels.
+--config NAME prints one of them (or c3d: the headline's refined solve on
+strided dense batches against the compact layout) on its own line; --no-extra
+leaves them out. --case KIND N NM runs one small solve for a profiler
+capture.
 """
 from __future__ import annotations
 
@@ -720,9 +724,14 @@ def run_gpu(args):
             lambda: [(b["n"], b["A"].cpu().numpy(), b["B"].cpu().numpy()) for b in batches])
     if not args.no_e2e:
         line["e2e"] = e2e(args, cbk, batches, barrier, ws)
-    # free the device before printing
+    # free the device, then the other configurations (1 GPU only)
     del batches
     torch.cuda.empty_cache()
+    if ws == 1 and not args.no_extra:
+        t0 = time.perf_counter()
+        line["configs"] = config_lines(("c1", "c2", "c4", "c5"), args, cbk, dev,
+                                       with_cpu=not args.no_cpu)
+        line["configs_wall_s"] = time.perf_counter() - t0
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -819,188 +828,335 @@ def _timer(dev):
     return run
 
 
-def run_config(args):
+def cpu_best_width(timer, sample_fn, widths=CPU_WIDTHS):
+    """The fastest of the reference's widths for one configuration: timer(Vc,
+    packed) -> seconds for one pass, sample_fn(Vc) -> the packed sample."""
+    t = {}
+    for Vc in widths:
+        pk = sample_fn(Vc)
+        timer(Vc, pk)
+        t[Vc] = min(timer(Vc, pk) for _ in range(2))
+    return min(t, key=t.get), {str(k): 1e3 * v for k, v in t.items()}
+
+
+def cpu_config_baseline(kind, dense, unit, steps=3):
+    """The reference's own CPU build (its performance build, every host core)
+    on one configuration's matrices, copied to the host: the fastest width of
+    2/4/8 on a 16384-matrix sample, then the whole batch, best of `steps`
+    passes with the inputs restored untimed before each call. dense holds
+    the configuration's host arrays; kind selects the calls:
+      posv  dense = (A, B): dposv_compact
+      gels  dense = (A, B): dgels_compact ('N')
+      sysvnp  dense = [(A_n, B_n) per order]: one dsysvnp_compact per order
+    Returns the cpu_baseline object (units: matrices per second)."""
+    import numpy as np
+    from oracle import oracle as O
+    lib, lkind = cpu_lib()
+
+    def pack_all(Vc, limit=None):
+        out = []
+        for A, B in (dense if kind == "sysvnp" else [dense]):
+            A_, B_ = (A, B) if limit is None else (A[:limit], B[:limit])
+            if A_.shape[0] == 0:
+                continue
+            a0, b0 = O.pack(A_, Vc), O.pack(B_, Vc, pad_diag=0.0)
+            out.append((A_.shape, B_.shape, a0, b0, a0.copy(), b0.copy()))
+        return out
+
+    def one_pass(Vc, packed):
+        t = 0.0
+        for (sa, sb, a0, b0, a, b) in packed:
+            np.copyto(a, a0)
+            np.copyto(b, b0)
+            nm, m, n = sa
+            nrhs = sb[2]
+            t0 = time.perf_counter()
+            if kind == "gels":
+                tau = np.zeros(O.compact_size(nm, n, 1, n, Vc))
+                info = lib.call("gels", np.float64, "C", "N", m, n, nrhs, a, m, b, m, tau, Vc, nm)
+            else:
+                info = lib.call(kind, np.float64, "C", "L", n, nrhs, a, n, b, n, Vc, nm)
+            t += time.perf_counter() - t0
+            assert info == 0, info
+        return t
+
+    per = 16384 if kind != "sysvnp" else 1024
+    Vc, wms = cpu_best_width(one_pass, lambda Vc: pack_all(Vc, per))
+    packed = pack_all(Vc)
+    total = sum(p[0][0] for p in packed)
+    one_pass(Vc, packed)
+    best = min(one_pass(Vc, packed) for _ in range(steps))
+    return {"value": total / best, "unit": unit, "cores": cpu_threads(), "kind": lkind, "V": Vc,
+            "width_ms_sample": wms, "ms_per_pass": 1e3 * best,
+            "sample": f"this configuration's own {total} matrices, copied to the host; "
+                      f"fastest width of {CPU_WIDTHS} on {per} per call; best of {steps}"}
+
+
+def fp64_peak(cbk):
+    """The measured FP64 FMA rate in TFLOP/s (cbk_cuda_measure_fma_rate)."""
+    return ctypes_fma_rate(cbk)
+
+
+def config_lines(names, args, cbk, dev, with_cpu=True):
+    """The other configurations' measurements, one dict per name (c1, c2, c4,
+    c5, c3d), each with its own roofline against the pipe that binds it (FP64
+    work over the measured FP64 FMA rate; algorithmic bytes over the measured
+    HBM copy rate) and, for c1 / c2 / c4 / c5, a cpu_baseline through the
+    reference's own build on the same matrices."""
     import numpy as np
     import torch
-
-    import cbk_gb300 as cbk
-    dev = torch.device("cuda", 0)
     gen = torch.Generator(device=dev)
     gen.manual_seed(SEED)
     timed = _timer(dev)
     f64 = torch.float64
-    line = {"metric": None, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    rate = fp64_peak(cbk)
+    hbm = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm = json.load(f).get("hbm_gbs")
+    except OSError:
+        pass
+    hbm_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+
+    def roof(flops, nbytes, ms, kernel):
+        tf = flops / (ms * 1e-3) / 1e12
+        gb = nbytes / (ms * 1e-3) / 1e9
+        return {"kernel": kernel, "bound": "fp64 pipe", "fp64_tflops": tf, "fp64_peak": rate,
+                "fp64_frac": tf / rate if rate else None, "hbm_gbs": gb, "hbm_peak": hbm,
+                "hbm_frac": gb / hbm, "peak_source": f"FP64: measured FMA rate this run; HBM: "
+                                                     f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)"}
+
+    out = {}
+    base = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
             "config": {"workload": None, "l2": "flushed (256 MiB write) before every timed step",
                        "inputs": "restored untimed before every step"}}
-    if args.config == "c1":
-        n, nm = 8, 65536
-        G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
-        A = G @ G.transpose(1, 2) + n * torch.eye(n, dtype=f64, device=dev)
-        B = torch.randn(nm, n, 1, dtype=f64, device=dev, generator=gen)
-        ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
-        ap, bp = ap0.clone(), bp0.clone()
-
-        def restore():
-            ap.copy_(ap0)
-            bp.copy_(bp0)
-        t, _ = timed(lambda: cbk.check("posv", cbk.dposv_compact("C", "L", n, 1, ap, n, bp, n, V,
-                                                                 nm)) or 1, restore,
-                     args.steps, args.warmup)
-        berr = berr_max(A, x_dense(bp, n, nm), B) / (n * 2.220446049250313e-16)
-        it = torch.empty(nm, dtype=torch.int32, device=dev)
-        tr, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
-            "C", "L", n, 1, ap, n, bp, n, V, nm, 10, it)) or 1, restore, args.steps, args.warmup)
-        line.update(metric="dposv_compact FP64 n=8 nrhs=1 solves/s", value=nm / (t * 1e-3),
-                    unit=UNIT, ms_per_step=t, dtype="f64",
-                    data="synthetic: A = G G^T + n I, G, B ~ N(0,1), seed 0x5EED",
-                    max_berr_over_n_eps=berr, refined_value=nm / (tr * 1e-3),
-                    gbs=nm * plain_bytes_per_matrix(n, 1) / (t * 1e-3) / 1e9,
-                    gpu_launches=args.steps)
-        line["config"]["workload"] = "dposv_compact n=8 nrhs=1, 65536 matrices, V=32"
-    elif args.config == "c2":
-        m, n, nrhs, nm = 16, 8, 4, 1 << 20
-        A = torch.randn(nm, m, n, dtype=f64, device=dev, generator=gen)
-        B = torch.randn(nm, m, nrhs, dtype=f64, device=dev, generator=gen)
-        ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
-        ap, bp = ap0.clone(), bp0.clone()
-        tau = torch.empty(nm * n, dtype=f64, device=dev)
-
-        def restore():
-            ap.copy_(ap0)
-            bp.copy_(bp0)
-        t, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact("C", "N", m, n, nrhs, ap, m, bp,
-                                                                 m, tau, V, nm)) or 1,
-                     restore, args.steps, args.warmup)
-        geq = ap.clone()  # the QR left by the last gels, for orgqr
-
-        def restore_q():
-            ap.copy_(geq)
-        tq, _ = timed(lambda: cbk.check("orgqr", cbk.dorgqr_compact("C", m, n, n, ap, m, tau, V,
-                                                                    nm)) or 1,
-                      restore_q, args.steps, args.warmup)
-        ng = nm // V
-        Q = ap.view(ng, n, m, V).permute(0, 3, 2, 1).reshape(nm, m, n)
-        orth = float((Q.transpose(1, 2) @ Q - torch.eye(n, dtype=f64, device=dev)).abs()
-                     .amax()) / 2.220446049250313e-16
-        line.update(metric="dgels_compact FP64 16x8 nrhs=4 solves/s", value=nm / (t * 1e-3),
-                    unit=UNIT, ms_per_step=t, dtype="f64", data="synthetic: A, B ~ N(0,1)",
-                    gbs=nm * 3136 / (t * 1e-3) / 1e9, dorgqr_ms=tq,
-                    dorgqr_per_s=nm / (tq * 1e-3), dorgqr_orthogonality_over_eps=orth,
-                    gpu_launches=args.steps)
-        line["config"]["workload"] = "dgels_compact m=16 n=8 nrhs=4 + dorgqr, 1048576, V=32"
-    elif args.config == "c4":
-        nrhs, total = 2, 1 << 20
-        rng = np.random.default_rng(SEED)
-        counts = np.bincount(rng.integers(4, 49, total), minlength=49)[4:]
-        bks = []
-        for k, n in enumerate(range(4, 49)):
-            nm = int(counts[k])
+    for name in names:
+        line = json.loads(json.dumps(base))
+        if name == "c1":
+            n, nm = 8, 65536
             G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
-            S = (G + G.transpose(1, 2)) / 2 + 2 * n * torch.eye(n, dtype=f64, device=dev)
-            Bm = torch.randn(nm, n, nrhs, dtype=f64, device=dev, generator=gen)
-            a0, b0 = pack_dev(cbk, S), pack_dev(cbk, Bm)
-            bks.append(dict(n=n, nm=nm, a0=a0, b0=b0, a=a0.clone(), b=b0.clone()))
-            del G, S, Bm
-
-        def restore():
-            for b in bks:
-                b["a"].copy_(b["a0"])
-                b["b"].copy_(b["b0"])
-        work = torch.empty(cbk.BUCKETED_LWORK, dtype=torch.uint8, device=dev)
-        tup = [(b["n"], b["nm"], V, b["a"], b["n"], b["b"], b["n"]) for b in bks]
-        graph = cbk.BucketedGraph("C", "L", nrhs, tup, work)
-        tg, _ = timed(lambda: cbk.check("graph", graph.launch()) or 1, restore, args.steps,
-                      args.warmup)
-
-        def per_size():
-            for b in bks:
-                cbk.check("sysvnp", cbk.dsysvnp_compact("C", "L", b["n"], nrhs, b["a"], b["n"],
-                                                        b["b"], b["n"], V, b["nm"]))
-            return len(bks)
-        tp, _ = timed(per_size, restore, args.steps, args.warmup)
-        graph.close()
-        line.update(metric="uneven-size dsysvnp solves/s (n~U{4..48}, nrhs=2)",
-                    value=total / (tg * 1e-3), unit=UNIT, ms_per_step=tg, dtype="f64",
-                    data="synthetic: symmetric N(0,1) + 2n I, B ~ N(0,1)",
-                    per_size_launches={"value": total / (tp * 1e-3), "ms_per_step": tp,
-                                       "launches": len(bks)},
-                    speedup_graph_vs_per_size=tp / tg, gpu_launches=args.steps)
-        line["config"]["workload"] = ("dsysvnp_compact, 1048576 matrices, n uniform in 4..48, "
-                                      "45 buckets, V=32: one persistent CUDA-graph launch")
-    elif args.config == "c3d":
-        # the headline batches as strided dense column-major arrays (lda = n,
-        # stride n^2): the refined solve reads and writes them in place,
-        # against the compact path on the same matrices
-        per, td_all, tc_all, same = {}, 0.0, 0.0, True
-        for n in SIZES:
-            A, B = gen_batch(n, NM, gen, dev)
-            a0, b0 = A.contiguous(), B.contiguous()
+            A = G @ G.transpose(1, 2) + n * torch.eye(n, dtype=f64, device=dev)
+            B = torch.randn(nm, n, 1, dtype=f64, device=dev, generator=gen)
             ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
-            del A, B
-            a, b, ap, bp = a0.clone(), b0.clone(), ap0.clone(), bp0.clone()
-            it = torch.empty(NM, dtype=torch.int32, device=dev)
+            ap, bp = ap0.clone(), bp0.clone()
 
-            def rd():
-                a.copy_(a0)
-                b.copy_(b0)
-
-            def rc():
+            def restore():
                 ap.copy_(ap0)
                 bp.copy_(bp0)
-            td, _ = timed(lambda: cbk.check("batched", cbk.dposv_refined_batched(
-                "L", n, NRHS, a, n, n * n, b, n, n * NRHS, NM, 10, it)) or 1, rd, args.steps,
+            t, _ = timed(lambda: cbk.check("posv", cbk.dposv_compact(
+                "C", "L", n, 1, ap, n, bp, n, V, nm)) or 1, restore, args.steps, args.warmup)
+            berr = berr_max(A, x_dense(bp, n, nm), B) / (n * 2.220446049250313e-16)
+            it = torch.empty(nm, dtype=torch.int32, device=dev)
+            tr, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
+                "C", "L", n, 1, ap, n, bp, n, V, nm, 10, it)) or 1, restore, args.steps,
                 args.warmup)
-            tc, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
-                "C", "L", n, NRHS, ap, n, bp, n, V, NM, 10, it)) or 1, rc, args.steps,
-                args.warmup)
-            same = same and torch.equal(b.view(NM, n), x_dense(bp, n, NM).view(NM, n))
-            per[str(n)] = {"dense_ms": td, "compact_ms": tc}
-            td_all += td
-            tc_all += tc
-            del a0, b0, ap0, bp0, a, b, ap, bp
-        line.update(metric="mixed-precision dposv on strided dense batches solves/s, n=8-48",
-                    value=NM * len(SIZES) / (td_all * 1e-3), unit=UNIT, ms_per_step=td_all,
-                    dtype="f32 factor + f64 refinement (f64 results)",
-                    data="synthetic: the headline's matrices (seed 0x5EED), dense column-major",
-                    compact={"value": NM * len(SIZES) / (tc_all * 1e-3), "ms_per_step": tc_all},
-                    per_n=per, x_bit_identical_to_compact=bool(same),
-                    gpu_launches=len(SIZES) * args.steps)
-        line["config"]["workload"] = ("dposv_refined_batched: n in {8,16,32,48}, 262144 matrices "
-                                      "each, A column-major lda = n, stride n^2, nrhs = 1")
-    elif args.config == "c5":
-        m, n, nrhs, nm = 64, 16, 8, 131072
-        ap0, bp0, Ad, Bd = ls_batch(m, n, nrhs, nm, dev)
-        ap, bp = ap0.clone(), bp0.clone()
-        tau = torch.empty(nm * n, dtype=f64, device=dev)
-        it = torch.empty(nm, dtype=torch.int32, device=dev)
-        work = torch.empty(cbk.dgels_refined_lwork(m, n, nrhs, V, nm), dtype=torch.uint8,
-                           device=dev)
+            line.update(metric="dposv_compact FP64 n=8 nrhs=1 solves/s", value=nm / (t * 1e-3),
+                        unit=UNIT, ms_per_step=t, dtype="f64",
+                        data="synthetic: A = G G^T + n I, G, B ~ N(0,1), seed 0x5EED",
+                        max_berr_over_n_eps=berr, refined_value=nm / (tr * 1e-3),
+                        gbs=nm * plain_bytes_per_matrix(n, 1) / (t * 1e-3) / 1e9,
+                        roofline=roof(nm * plain_flops(n), nm * plain_bytes_per_matrix(n, 1), t,
+                                      "k_chol_small<double,8,1>"),
+                        gpu_launches=args.steps)
+            line["config"]["workload"] = "dposv_compact n=8 nrhs=1, 65536 matrices, V=32"
+            if with_cpu:
+                line["cpu_baseline"] = cpu_config_baseline(
+                    "posv", (A.cpu().numpy(), B.cpu().numpy()), UNIT)
+            del A, B, G, ap0, bp0, ap, bp
+        elif name == "c2":
+            m, n, nrhs, nm = 16, 8, 4, 1 << 20
+            A = torch.randn(nm, m, n, dtype=f64, device=dev, generator=gen)
+            B = torch.randn(nm, m, nrhs, dtype=f64, device=dev, generator=gen)
+            ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+            ap, bp = ap0.clone(), bp0.clone()
+            tau = torch.empty(nm * n, dtype=f64, device=dev)
 
-        def restore():
-            ap.copy_(ap0)
-            bp.copy_(bp0)
-        tr, _ = timed(lambda: cbk.check("gels_refined", cbk.dgels_refined_compact(
-            "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm, 10, it, None, work)) or 1, restore,
-            args.steps, args.warmup)
-        itc = it.cpu().numpy()
-        ne_ref = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
-        tpl, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact("C", "N", m, n, nrhs, ap, m,
-                                                                   bp, m, tau, V, nm)) or 1,
-                       restore, args.steps, args.warmup)
-        ne_pl = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
-        line.update(metric="least squares 64x16 nrhs=8 solves/s: refined FP32 vs plain FP64",
-                    value=nm / (tr * 1e-3), unit=UNIT, ms_per_step=tr,
-                    dtype="f32 QR + f64 refinement", data="synthetic: A = U diag(s) V^T, kappa "
-                    "1e1..1e4, B = A X + 1e-3 N(0,1)",
-                    plain_fp64={"value": nm / (tpl * 1e-3), "ms_per_step": tpl},
-                    speedup_refined_vs_plain=tpl / tr,
-                    max_normal_residual_over_n_eps={"refined": ne_ref / (n * 2.220446049250313e-16),
-                                                    "plain": ne_pl / (n * 2.220446049250313e-16)},
-                    refinement={"converged_frac": float((itc >= 0).mean()),
-                                "mean_steps": float(itc[itc >= 0].mean())},
-                    gpu_launches=args.steps)
-        line["config"]["workload"] = "dgels m=64 n=16 nrhs=8, 131072 matrices, V=32"
+            def restore():
+                ap.copy_(ap0)
+                bp.copy_(bp0)
+            t, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact(
+                "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm)) or 1, restore, args.steps,
+                args.warmup)
+            geq = ap.clone()  # the QR left by the last gels, for orgqr
+
+            def restore_q():
+                ap.copy_(geq)
+            tq, _ = timed(lambda: cbk.check("orgqr", cbk.dorgqr_compact(
+                "C", m, n, n, ap, m, tau, V, nm)) or 1, restore_q, args.steps, args.warmup)
+            ng = nm // V
+            Q = ap.view(ng, n, m, V).permute(0, 3, 2, 1).reshape(nm, m, n)
+            orth = float((Q.transpose(1, 2) @ Q - torch.eye(n, dtype=f64, device=dev)).abs()
+                         .amax()) / 2.220446049250313e-16
+            del Q, geq
+            line.update(metric="dgels_compact FP64 16x8 nrhs=4 solves/s", value=nm / (t * 1e-3),
+                        unit=UNIT, ms_per_step=t, dtype="f64", data="synthetic: A, B ~ N(0,1)",
+                        gbs=nm * 3136 / (t * 1e-3) / 1e9, dorgqr_ms=tq,
+                        dorgqr_per_s=nm / (tq * 1e-3), dorgqr_orthogonality_over_eps=orth,
+                        roofline=roof(nm * 3499.0, nm * 3136.0, t, "k_gels<double>"),
+                        dorgqr_roofline=roof(nm * 1707.0, nm * 2112.0, tq, "k_orgqr<double>"),
+                        gpu_launches=args.steps)
+            line["config"]["workload"] = "dgels_compact m=16 n=8 nrhs=4 + dorgqr, 1048576, V=32"
+            if with_cpu:
+                line["cpu_baseline"] = cpu_config_baseline(
+                    "gels", (A.cpu().numpy(), B.cpu().numpy()), UNIT)
+            del A, B, ap0, bp0, ap, bp, tau
+        elif name == "c4":
+            nrhs, total = 2, 1 << 20
+            rng = np.random.default_rng(SEED)
+            counts = np.bincount(rng.integers(4, 49, total), minlength=49)[4:]
+            bks, host = [], []
+            flops = nbytes = 0.0
+            for k, n in enumerate(range(4, 49)):
+                nm = int(counts[k])
+                G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
+                S = (G + G.transpose(1, 2)) / 2 + 2 * n * torch.eye(n, dtype=f64, device=dev)
+                Bm = torch.randn(nm, n, nrhs, dtype=f64, device=dev, generator=gen)
+                a0, b0 = pack_dev(cbk, S), pack_dev(cbk, Bm)
+                bks.append(dict(n=n, nm=nm, a0=a0, b0=b0, a=a0.clone(), b=b0.clone()))
+                if with_cpu:
+                    host.append((S.cpu().numpy(), Bm.cpu().numpy()))
+                flops += nm * (n ** 3 / 3 + 2 * n * n * nrhs + n * nrhs)
+                nbytes += nm * 8 * (n * (n + 1) + 2 * n * nrhs)
+                del G, S, Bm
+
+            def restore():
+                for b in bks:
+                    b["a"].copy_(b["a0"])
+                    b["b"].copy_(b["b0"])
+            work = torch.empty(cbk.BUCKETED_LWORK, dtype=torch.uint8, device=dev)
+            tup = [(b["n"], b["nm"], V, b["a"], b["n"], b["b"], b["n"]) for b in bks]
+            graph = cbk.BucketedGraph("C", "L", nrhs, tup, work)
+            tg, _ = timed(lambda: cbk.check("graph", graph.launch()) or 1, restore, args.steps,
+                          args.warmup)
+
+            def per_size():
+                for b in bks:
+                    cbk.check("sysvnp", cbk.dsysvnp_compact("C", "L", b["n"], nrhs, b["a"],
+                                                            b["n"], b["b"], b["n"], V, b["nm"]))
+                return len(bks)
+            tp, _ = timed(per_size, restore, args.steps, args.warmup)
+            graph.close()
+            line.update(metric="uneven-size dsysvnp solves/s (n~U{4..48}, nrhs=2)",
+                        value=total / (tg * 1e-3), unit=UNIT, ms_per_step=tg, dtype="f64",
+                        data="synthetic: symmetric N(0,1) + 2n I, B ~ N(0,1)",
+                        per_size_launches={"value": total / (tp * 1e-3), "ms_per_step": tp,
+                                           "launches": len(bks)},
+                        speedup_graph_vs_per_size=tp / tg,
+                        roofline=roof(flops, nbytes, tg, "k_bucketed<double,true>"),
+                        gpu_launches=args.steps)
+            line["config"]["workload"] = ("dsysvnp_compact, 1048576 matrices, n uniform in "
+                                          "4..48, 45 buckets, V=32: one persistent CUDA-graph "
+                                          "launch")
+            if with_cpu:
+                line["cpu_baseline"] = cpu_config_baseline("sysvnp", host, UNIT)
+                line["cpu_baseline"]["sample"] += " (one call per order, as the reference takes)"
+            del bks, host, work
+        elif name == "c3d":
+            # the headline batches as strided dense column-major arrays (lda =
+            # n, stride n^2): the refined solve reads and writes them in place,
+            # against the compact path on the same matrices
+            per, td_all, tc_all, same = {}, 0.0, 0.0, True
+            for n in SIZES:
+                A, B = gen_batch(n, NM, gen, dev)
+                a0, b0 = A.contiguous(), B.contiguous()
+                ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+                del A, B
+                a, b, ap, bp = a0.clone(), b0.clone(), ap0.clone(), bp0.clone()
+                it = torch.empty(NM, dtype=torch.int32, device=dev)
+
+                def rd():
+                    a.copy_(a0)
+                    b.copy_(b0)
+
+                def rc():
+                    ap.copy_(ap0)
+                    bp.copy_(bp0)
+                td, _ = timed(lambda: cbk.check("batched", cbk.dposv_refined_batched(
+                    "L", n, NRHS, a, n, n * n, b, n, n * NRHS, NM, 10, it)) or 1, rd,
+                    args.steps, args.warmup)
+                tc, _ = timed(lambda: cbk.check("posv_refined", cbk.dposv_refined_compact(
+                    "C", "L", n, NRHS, ap, n, bp, n, V, NM, 10, it)) or 1, rc, args.steps,
+                    args.warmup)
+                same = same and torch.equal(b.view(NM, n), x_dense(bp, n, NM).view(NM, n))
+                per[str(n)] = {"dense_ms": td, "compact_ms": tc}
+                td_all += td
+                tc_all += tc
+                del a0, b0, ap0, bp0, a, b, ap, bp
+            line.update(metric="mixed-precision dposv on strided dense batches solves/s, n=8-48",
+                        value=NM * len(SIZES) / (td_all * 1e-3), unit=UNIT, ms_per_step=td_all,
+                        dtype="f32 factor + f64 refinement (f64 results)",
+                        data="synthetic: the headline's matrices (seed 0x5EED), dense "
+                             "column-major",
+                        compact={"value": NM * len(SIZES) / (tc_all * 1e-3),
+                                 "ms_per_step": tc_all},
+                        per_n=per, x_bit_identical_to_compact=bool(same),
+                        gpu_launches=len(SIZES) * args.steps)
+            line["config"]["workload"] = ("dposv_refined_batched: n in {8,16,32,48}, 262144 "
+                                          "matrices each, A column-major lda = n, stride n^2, "
+                                          "nrhs = 1")
+        elif name == "c5":
+            m, n, nrhs, nm = 64, 16, 8, 131072
+            ap0, bp0, Ad, Bd = ls_batch(m, n, nrhs, nm, dev)
+            ap, bp = ap0.clone(), bp0.clone()
+            tau = torch.empty(nm * n, dtype=f64, device=dev)
+            it = torch.empty(nm, dtype=torch.int32, device=dev)
+            work = torch.empty(cbk.dgels_refined_lwork(m, n, nrhs, V, nm), dtype=torch.uint8,
+                               device=dev)
+
+            def restore():
+                ap.copy_(ap0)
+                bp.copy_(bp0)
+            tr, _ = timed(lambda: cbk.check("gels_refined", cbk.dgels_refined_compact(
+                "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm, 10, it, None, work)) or 1,
+                restore, args.steps, args.warmup)
+            itc = it.cpu().numpy()
+            ne_ref = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
+            tpl, _ = timed(lambda: cbk.check("gels", cbk.dgels_compact(
+                "C", "N", m, n, nrhs, ap, m, bp, m, tau, V, nm)) or 1, restore, args.steps,
+                args.warmup)
+            ne_pl = ls_normal_residual(Ad, bp, Bd, m, n, nrhs, nm)
+            steps = float(itc[itc >= 0].mean())
+            # FP64 work of the refined solve: per right-hand side and step the
+            # residuals f = b - r - A x (2mn, skipped at the first step) and
+            # g = -A^T r (2mn); plain: geqrf + Q^T B + R^-1
+            fl_ref = nm * nrhs * (4.0 * m * n * (steps + 1) - 2.0 * m * n)
+            fl_pl = nm * (2 * m * n * n - 2 * n ** 3 / 3 + 4 * m * nrhs * n - 2 * nrhs * n * n +
+                          n * n * nrhs)
+            by = nm * 8 * (m * n + 2 * m * nrhs)
+            eps = 2.220446049250313e-16
+            line.update(metric="least squares 64x16 nrhs=8 solves/s: refined FP32 vs plain FP64",
+                        value=nm / (tr * 1e-3), unit=UNIT, ms_per_step=tr,
+                        dtype="f32 QR + f64 refinement", data="synthetic: A = U diag(s) V^T, "
+                        "kappa 1e1..1e4, B = A X + 1e-3 N(0,1)",
+                        plain_fp64={"value": nm / (tpl * 1e-3), "ms_per_step": tpl,
+                                    "roofline": roof(fl_pl, nm * 8 * (2 * m * n + n + 2 * m *
+                                                                     nrhs), tpl, "k_gels<double>")},
+                        speedup_refined_vs_plain=tpl / tr,
+                        max_normal_residual_over_n_eps={"refined": ne_ref / (n * eps),
+                                                        "plain": ne_pl / (n * eps)},
+                        refinement={"converged_frac": float((itc >= 0).mean()),
+                                    "mean_steps": steps},
+                        roofline=roof(fl_ref, by, tr, "k_gels_refined_warp<2,16,4,3>"),
+                        gpu_launches=args.steps)
+            line["config"]["workload"] = "dgels m=64 n=16 nrhs=8, 131072 matrices, V=32"
+            if with_cpu:
+                line["cpu_baseline"] = cpu_config_baseline(
+                    "gels", (Ad.cpu().numpy(), Bd.cpu().numpy()), UNIT)
+                line["cpu_baseline"]["sample"] += " (the reference's plain FP64 dgels_compact)"
+            del ap0, bp0, Ad, Bd, ap, bp, tau, work
+        torch.cuda.empty_cache()
+        out[name] = line
+    return out
+
+
+def run_config(args):
+    import torch
+
+    import cbk_gb300 as cbk
+    dev = torch.device("cuda", 0)
+    line = config_lines([args.config], args, cbk, dev, with_cpu=not args.no_cpu)[args.config]
     print(json.dumps(line), flush=True)
 
 
@@ -1014,6 +1170,8 @@ def main():
                     help="keep the built-in launch shapes instead of autotuning them first")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the other configurations (c1, c2, c4, c5) in the headline line")
     ap.add_argument("--ref-per-n", type=int, default=NM,
                     help="--impl reference: matrices per order (default: the whole workload)")
     ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5", "c3d"), default="c3",
