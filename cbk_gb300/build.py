@@ -49,20 +49,29 @@ def _stale(src: str, obj: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in [src] + deps)
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile and link; returns the library path."""
-    os.makedirs(BUILD, exist_ok=True)
+LIB_CHECKED = os.path.join(PKG, "libcbk_cuda_checked.so")
+
+
+def build(verbose: bool = False, jobs: int | None = None, checked: bool = False) -> str:
+    """Compile and link; returns the library path. checked=True builds the
+    bounds-checked variant (CBK_CUDA_CHECKED; libcbk_cuda_checked.so, objects
+    in _build/checked): every matrix-view access tested against its extent,
+    for the tests, not for speed."""
+    build_dir = os.path.join(BUILD, "checked") if checked else BUILD
+    lib_path = LIB_CHECKED if checked else LIB
+    flags = NVCC_FLAGS + (["-DCBK_CUDA_CHECKED"] if checked else [])
+    os.makedirs(build_dir, exist_ok=True)
     cc = nvcc()
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     deps = _headers()
     objs = []
     todo = []
     for src in sources:
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(src, obj, deps):
             lang = [] if src.endswith(".cu") else ["-x", "cu"]
-            todo.append([cc, "-c"] + lang + NVCC_FLAGS + [src, "-o", obj])
+            todo.append([cc, "-c"] + lang + flags + [src, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -76,14 +85,14 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         for msg in ex.map(run, todo):
             if verbose and msg:
                 print(msg)
-    if todo or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB)
-                                              for o in objs):
-        tmp = LIB + ".tmp"
+    if todo or not os.path.exists(lib_path) or any(
+            os.path.getmtime(o) > os.path.getmtime(lib_path) for o in objs):
+        tmp = lib_path + ".tmp"
         run([cc, "-shared"] + ARCH + ["-cudart", "static", "-o", tmp] + objs)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
     import sys
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -13,6 +13,33 @@
 
 #include <cuda_runtime.h>
 
+#ifdef CBK_CUDA_CHECKED
+// The checked build's status words: every translation unit that includes the
+// device header registers a reader of its own word at load time.
+namespace cbkcuda {
+typedef int (*CheckReader)(unsigned long long *count, unsigned long long *first, int reset);
+namespace {
+constexpr int MAX_READERS = 64;
+struct Readers {
+    CheckReader r[MAX_READERS];
+    int n = 0;
+};
+Readers &readers()
+{
+    static Readers g;
+    return g;
+}
+} // namespace
+void register_check_reader(CheckReader r)
+{
+    Readers &g = readers();
+    if (g.n < MAX_READERS) g.r[g.n++] = r;
+}
+inline const CheckReader *check_readers() { return readers().r; }
+inline int check_readers_n() { return readers().n; }
+} // namespace cbkcuda
+#endif
+
 namespace {
 
 using namespace cbkcuda;
@@ -372,6 +399,28 @@ int cbk_cuda_get_version(void)
 int cbk_cuda_vlen_ok(int V)
 {
     return vlen_ok(V) ? 1 : 0;
+}
+
+int cbk_cuda_check_status(unsigned long long *count, int *first_i, int *first_j, int reset)
+{
+    unsigned long long total = 0, first = 0;
+    int rc = 0;
+#ifdef CBK_CUDA_CHECKED
+    for (int k = 0; k < cbkcuda::check_readers_n(); ++k) {
+        unsigned long long c = 0, f = 0;
+        const int e = cbkcuda::check_readers()[k](&c, &f, reset);
+        if (e != 0 && rc == 0) rc = CBK_CUDA_ERROR_BASE + e;
+        if (c != 0 && total == 0) first = f;
+        total += c;
+    }
+#else
+    (void)reset;
+    rc = -1;
+#endif
+    if (count) *count = total;
+    if (first_i) *first_i = (int)(unsigned)(first >> 32);
+    if (first_j) *first_j = (int)(unsigned)(first & 0xffffffffull);
+    return rc;
 }
 
 const char *cbk_cuda_status_string(int info)

@@ -30,22 +30,127 @@
 
 namespace cbkdev {
 
+// ---------------------------------------------------------------------
+// The checked build (CBK_CUDA_CHECKED defined: libcbk_cuda_checked.so)
+// ---------------------------------------------------------------------
+// Every element access through a matrix view (LV below) is tested against
+// the matrix's logical extent -- 0 <= i < rows, 0 <= j < cols of the view --
+// before it is made. An access outside is not made: it reads or writes a
+// scratch element instead, counts itself in this translation unit's status
+// word and records its (i, j) if it was the first; the host reads the words
+// through cbk_cuda_check_status. No trap, no fault: the kernel runs on. The
+// normal build compiles none of this (the view carries no extent).
+#ifdef CBK_CUDA_CHECKED
+struct CheckWord {
+    unsigned long long count; // accesses outside their view
+    unsigned long long first; // (i << 32) | j of the first, as unsigned 32-bit halves
+};
+static __device__ CheckWord g_check;
+static __device__ double g_check_scratch;
+// the host side keeps its own scratch and word (host-side uses of a view)
+inline CheckWord &host_check_word()
+{
+    static CheckWord w{0, 0};
+    return w;
+}
+inline double &host_check_scratch()
+{
+    static double d = 0.0;
+    return d;
+}
+
+template <typename T> __host__ __device__ inline T &check_fail(int i, int j)
+{
+    const unsigned long long code = ((unsigned long long)(unsigned)i << 32) | (unsigned)j;
+#ifdef __CUDA_ARCH__
+    if (atomicAdd(&g_check.count, 1ull) == 0ull) g_check.first = code;
+    return *reinterpret_cast<T *>(&g_check_scratch);
+#else
+    if (host_check_word().count++ == 0) host_check_word().first = code;
+    return *reinterpret_cast<T *>(&host_check_scratch());
+#endif
+}
+#endif
+
+#ifdef CBK_CUDA_CHECKED
+} // namespace cbkdev
+
+namespace cbkcuda {
+// one reader per translation unit's status word; cbk_cuda_check_status sums
+// them (count; first (i, j) of the first unit that has one; reset to zero)
+typedef int (*CheckReader)(unsigned long long *count, unsigned long long *first, int reset);
+void register_check_reader(CheckReader r);
+} // namespace cbkcuda
+
+namespace {
+int cbk_check_read_unit(unsigned long long *count, unsigned long long *first, int reset)
+{
+    cbkdev::CheckWord w{0, 0};
+    cudaError_t e = cudaMemcpyFromSymbol(&w, cbkdev::g_check, sizeof w);
+    if (e == cudaSuccess && reset) {
+        const cbkdev::CheckWord z{0, 0};
+        e = cudaMemcpyToSymbol(cbkdev::g_check, &z, sizeof z);
+    }
+    *count = w.count;
+    *first = w.first;
+    return (int)e;
+}
+const bool cbk_check_registered = (cbkcuda::register_check_reader(&cbk_check_read_unit), true);
+} // namespace
+
+namespace cbkdev {
+#endif
+
 // A strided view of one lane's matrix: element (i,j) at p[i*si + j*sj], the
-// strides in scalars (the compact pack stride times V).
+// strides in scalars (the compact pack stride times V); in the checked build
+// also the logical extent rows x cols.
 template <typename T> struct LV {
     T *p;
     long si, sj;
-    __device__ __forceinline__ T &operator()(int i, int j) const
+#ifdef CBK_CUDA_CHECKED
+    int rows, cols;
+#endif
+    __host__ __device__ __forceinline__ T &operator()(int i, int j) const
     {
+#ifdef CBK_CUDA_CHECKED
+        if ((unsigned)i >= (unsigned)rows || (unsigned)j >= (unsigned)cols)
+            return check_fail<T>(i, j);
+#endif
         return p[(long)i * si + (long)j * sj];
     }
-    __device__ __forceinline__ LV t() const { return {p, sj, si}; }
+    __host__ __device__ __forceinline__ LV t() const
+    {
+#ifdef CBK_CUDA_CHECKED
+        return {p, sj, si, cols, rows};
+#else
+        return {p, sj, si};
+#endif
+    }
 };
 
-template <typename T>
-__device__ __forceinline__ LV<T> lv_make(T *p, bool row, int ld, int V)
+// The same view from column `first` on (columns first .. cols-1 become 0 ..)
+template <typename T> __host__ __device__ __forceinline__ LV<T> lv_from_col(LV<T> v, int first)
 {
+    v.p += (long)first * v.sj;
+#ifdef CBK_CUDA_CHECKED
+    v.cols -= first;
+#endif
+    return v;
+}
+
+// The view of a lane's rows x cols matrix stored with leading dimension ld
+// (column-major, or row-major when row), V lanes interleaved.
+template <typename T>
+__host__ __device__ __forceinline__ LV<T> lv_make(T *p, bool row, int ld, int V, int rows, int cols)
+{
+#ifdef CBK_CUDA_CHECKED
+    return row ? LV<T>{p, (long)ld * V, (long)V, rows, cols}
+               : LV<T>{p, (long)V, (long)ld * V, rows, cols};
+#else
+    (void)rows;
+    (void)cols;
     return row ? LV<T>{p, (long)ld * V, (long)V} : LV<T>{p, (long)V, (long)ld * V};
+#endif
 }
 
 // Scalars per group of V interleaved rows x cols matrices.
@@ -637,8 +742,7 @@ __device__ __forceinline__ void gels_fallback_lane(int m, int n, int nrhs, int f
 {
     geqrf_lane<double>(m, n, A, taup, V);
     if (first < nrhs) {
-        LV<double> Bs = B;
-        Bs.p += (long)first * B.sj;
+        const LV<double> Bs = lv_from_col(B, first);
         ormqr_lane<double>(true, m, nrhs - first, n, A, taup, V, Bs);
         trsm_lane<double>(true, true, false, false, n, nrhs - first, 1.0, A, Bs);
     }

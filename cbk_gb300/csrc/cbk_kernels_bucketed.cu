@@ -58,12 +58,12 @@ __global__ void __launch_bounds__(128) k_bucketed(const __grid_constant__ Bucket
         const int V = tab.V[b], n = tab.n[b];
         const long g = l / V;
         const int v = (int)(l - g * V);
-        LV<T> A = lv_make<T>(tab.ap[b] + g * tab.sa[b] + v, row, tab.ldap[b], V);
+        LV<T> A = lv_make<T>(tab.ap[b] + g * tab.sa[b] + v, row, tab.ldap[b], V, n, n);
         if (up) A = A.t();
         factor_lane<T, LDLT>(n, A);
         if (nrhs > 0)
             sym_solve_lane<T, LDLT>(n, nrhs, A,
-                                    lv_make<T>(tab.bp[b] + g * tab.sb[b] + v, row, tab.ldbp[b], V));
+                                    lv_make<T>(tab.bp[b] + g * tab.sb[b] + v, row, tab.ldbp[b], V, n, nrhs));
     }
 }
 

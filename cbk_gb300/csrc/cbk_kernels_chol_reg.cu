@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(128)
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, N, N);
     if (up) A = A.t();
     T a[N][N]; // the lower triangle, a[i][j] for j <= i
 #pragma unroll
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int i = 0; i < N; ++i)
         rinv[i] = rcp(a[i][i]);
-    const LV<T> B = lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V);
+    const LV<T> B = lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, N, nrhs);
     for (int c = 0; c < nrhs; ++c) {
         T x[N];
 #pragma unroll

@@ -26,7 +26,7 @@ __global__ void k_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, lon
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    zero_lane<T>(lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V), 0, rows, cols);
+    zero_lane<T>(lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, rows, cols), 0, rows, cols);
 }
 
 template <typename T, bool LDLT>
@@ -34,7 +34,7 @@ __global__ void k_factor(bool row, bool up, int n, T *ap, int ldap, int V, long 
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, n, n);
     if (up) A = A.t();
     factor_lane<T, LDLT>(n, A);
 }
@@ -45,10 +45,10 @@ __global__ void k_sym_solve(bool row, bool up, int n, int nrhs, T *ap, int ldap,
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, n, n);
     if (up) A = A.t();
     if (FUSED) factor_lane<T, LDLT>(n, A);
-    sym_solve_lane<T, LDLT>(n, nrhs, A, lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V));
+    sym_solve_lane<T, LDLT>(n, nrhs, A, lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, n, nrhs));
 }
 
 template <typename T>
@@ -58,9 +58,10 @@ __global__ void k_trsm(bool left, bool up, bool row, bool tran, bool unit, int m
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    const LV<T> A = lv_make<T>(const_cast<T *>(ap) + ln.g * sa + ln.v, row, ldap, V);
+    const int s = left ? m : n;
+    const LV<T> A = lv_make<T>(const_cast<T *>(ap) + ln.g * sa + ln.v, row, ldap, V, s, s);
     trsm_lane<T>(left, up, tran, unit, m, n, alpha, A,
-                 lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V));
+                 lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, m, n));
 }
 
 template <typename T>
@@ -69,7 +70,8 @@ __global__ void k_geqrf(bool row, int m, int n, T *ap, int ldap, T *taup, int V,
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    geqrf_lane<T>(m, n, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V), taup + ln.g * st + ln.v, V);
+    geqrf_lane<T>(m, n, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, m, n),
+                  taup + ln.g * st + ln.v, V);
 }
 
 template <typename T>
@@ -79,8 +81,9 @@ __global__ void k_ormqr(bool left, bool row, bool forward, int m, int n, int k, 
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    const LV<T> A = lv_make<T>(const_cast<T *>(ap) + ln.g * sa + ln.v, row, ldap, V);
-    LV<T> C = lv_make<T>(cp + ln.g * sc + ln.v, row, ldcp, V);
+    const LV<T> A =
+        lv_make<T>(const_cast<T *>(ap) + ln.g * sa + ln.v, row, ldap, V, left ? m : n, k);
+    LV<T> C = lv_make<T>(cp + ln.g * sc + ln.v, row, ldcp, V, m, n);
     if (!left) C = C.t();
     ormqr_lane<T>(forward, left ? m : n, left ? n : m, k, A, taup + ln.g * st + ln.v, V, C);
 }
@@ -91,7 +94,7 @@ __global__ void k_orgqr(bool row, int m, int n, int k, T *ap, int ldap, const T 
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    orgqr_lane<T>(m, n, k, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V),
+    orgqr_lane<T>(m, n, k, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, m, n),
                   taup + ln.g * st + ln.v, V);
 }
 
@@ -102,10 +105,10 @@ __global__ void k_gels(bool row, bool tall, bool overdet, int p, int q, int nrhs
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, tall ? p : q, tall ? q : p);
     if (!tall) A = A.t();
     gels_lane<T>(overdet, p, q, nrhs, A, taup + ln.g * st + ln.v, V,
-                 lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V));
+                 lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, p, nrhs));
 }
 
 } // namespace

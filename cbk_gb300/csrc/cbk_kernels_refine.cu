@@ -81,8 +81,7 @@ __device__ __noinline__ void fallback_lane(int n, int nrhs, int first, LV<double
 {
     factor_lane<double, false>(n, A);
     if (first < nrhs) {
-        LV<double> Bs = B;
-        Bs.p += (long)first * B.sj;
+        const LV<double> Bs = lv_from_col(B, first);
         sym_solve_lane<double, false>(n, nrhs - first, A, Bs);
     }
 }
@@ -130,9 +129,9 @@ __global__ void __launch_bounds__(128)
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
     const long idx = ln.g * V + ln.v;
-    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V, N, N);
     if (up) A = A.t();
-    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
+    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V, N, nrhs);
 
     // FP64 <-> FP32 conversions and range tests are integer operations here:
     // a hardware conversion or FP64 compare takes an FP64-pipe slot
@@ -300,13 +299,14 @@ __global__ void __launch_bounds__(128, 4)
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
     const long idx = ln.g * V + ln.v;
-    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V);
+    LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V, n, n);
     if (up) A = A.t();
-    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
-    const LV<float> W = lv_make<float>(w.L + ln.g * ((size_t)n * n * V) + ln.v, false, n, V);
+    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V, n, nrhs);
+    const LV<float> W =
+        lv_make<float>(w.L + ln.g * ((size_t)n * n * V) + ln.v, false, n, V, n, n);
     double *X = w.x + ln.g * ((size_t)n * V) + ln.v;
     float *Z = w.z + ln.g * ((size_t)n * V) + ln.v;
-    const LV<float> Zv{Z, (long)V, 0};
+    const LV<float> Zv = lv_make<float>(Z, false, n, V, n, 1);
 
     int status = 0;
     for (int j = 0; j < n; ++j)

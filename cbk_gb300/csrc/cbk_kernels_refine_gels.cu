@@ -58,14 +58,15 @@ __global__ void __launch_bounds__(128, 4)
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
     const long idx = ln.g * V + ln.v;
-    const LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V);
-    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V);
+    const LV<double> A = lv_make<double>(ap + ln.g * sa + ln.v, row, ldap, V, m, n);
+    const LV<double> B = lv_make<double>(bp + ln.g * sb + ln.v, row, ldbp, V, m, nrhs);
     double *tau64 = taup + ln.g * ((size_t)n * V) + ln.v;
-    const LV<float> Q = lv_make<float>(w.a + ln.g * ((size_t)m * n * V) + ln.v, false, m, V);
+    const LV<float> Q =
+        lv_make<float>(w.a + ln.g * ((size_t)m * n * V) + ln.v, false, m, V, m, n);
     float *t32 = w.tau + ln.g * ((size_t)n * V) + ln.v;
     float *W = w.w + ln.g * ((size_t)m * V) + ln.v;
     double *R = w.r + ln.g * ((size_t)m * V) + ln.v;
-    const LV<float> Wv{W, (long)V, 0}; // the work vector as an m x 1 view
+    const LV<float> Wv = lv_make<float>(W, false, m, V, m, 1); // the work vector, m x 1
 
     int status = 0;
     for (int j = 0; j < n; ++j)

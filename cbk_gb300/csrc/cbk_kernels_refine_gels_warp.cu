@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(32 * WPB, MINB)
         if (i < m) {
             const long g = idx / V;
             const int v = (int)(idx - g * V);
-            const LV<double> A = lv_make<double>(ap + g * sa + v, row, ldap, V);
+            const LV<double> A = lv_make<double>(ap + g * sa + v, row, ldap, V, m, N);
             cp_async8(dst, &A(i, j));
         }
         else {
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(32 * WPB, MINB)
     float *sT = reinterpret_cast<float *>(ws + G::OFF_T);
     const long g = idx / V;
     const int v = (int)(idx - g * V);
-    const LV<double> B = lv_make<double>(bp + g * sb + v, row, ldbp, V);
+    const LV<double> B = lv_make<double>(bp + g * sb + v, row, ldbp, V, m, nrhs);
     const int jg = lane >> S;        // this lane's column in the column-wise phases
     const int hb = lane & (HB - 1);  // its row phase in A^T r
     int status = 0;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(32 * WPB, MINB)
         __syncwarp();
     }
     if (status != 0 && lane == 0) {
-        const LV<double> A = lv_make<double>(ap + g * sa + v, row, ldap, V);
+        const LV<double> A = lv_make<double>(ap + g * sa + v, row, ldap, V, m, N);
         gels_fallback_lane(m, N, nrhs, status == -3 ? col - 1 : 0, A,
                            taup + g * ((size_t)N * V) + v, V, B);
     }

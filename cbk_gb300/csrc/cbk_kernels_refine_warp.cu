@@ -169,8 +169,7 @@ __device__ __forceinline__ void warp_fallback(int n, int nrhs, int first, LV<dou
 {
     factor_lane<double, false>(n, A);
     if (first < nrhs) {
-        LV<double> Bs = B;
-        Bs.p += (long)first * B.sj;
+        const LV<double> Bs = lv_from_col(B, first);
         sym_solve_lane<double, false>(n, nrhs - first, A, Bs);
     }
 }
@@ -339,7 +338,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     // a warp's copies cover WPB neighbouring lanes of eight rows (whole 32-byte
     // sectors), and its shared-memory writes two wavefronts.
     {
-        LV<double> A0 = lv_make<double>(ap, row, ldap, V);
+        LV<double> A0 = lv_make<double>(ap, row, ldap, V, n, n);
         if (up) A0 = A0.t();
         const int w = threadIdx.x % WPB, rr = threadIdx.x / WPB;
         const bool have = m0 + w < nlanes;
@@ -379,9 +378,9 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
     if (m >= nlanes) return;
     const long g = m / V;
     const int v = (int)(m - g * V);
-    LV<double> Ag = lv_make<double>(ap + g * sa + v, row, ldap, V);
+    LV<double> Ag = lv_make<double>(ap + g * sa + v, row, ldap, V, n, n);
     if (up) Ag = Ag.t();
-    const LV<double> B = lv_make<double>(bp + g * sb + v, row, ldbp, V);
+    const LV<double> B = lv_make<double>(bp + g * sb + v, row, ldbp, V, n, nrhs);
 
     // ---- the scaling D and the FP32 rows of D A D; ||A||_inf of the n rows ----
     int h[NR]; // D(i, i) = 2^-h

@@ -481,6 +481,19 @@ void cbk_cuda_tune_reset(void);
 int cbk_cuda_tune_save(const char *path);
 int cbk_cuda_tune_load(const char *path);
 
+/* The bounds-checked build, no reference counterpart. libcbk_cuda_checked.so
+ * (cbk_gb300/build.py, build(checked=True)) is this library compiled with
+ * CBK_CUDA_CHECKED: every element access a kernel makes through a matrix
+ * view -- all of the lane-per-matrix kernels' accesses, and the warp
+ * kernels' global-memory ones -- is first tested against the matrix's
+ * logical extent; an access outside it is not made but counted, with the
+ * (i, j) of the first. cbk_cuda_check_status reads (and, if reset, clears)
+ * that count after the caller has synchronised its streams. Returns 0, -1 in
+ * the normal build (count 0: nothing is checked), or CBK_CUDA_ERROR_BASE + a
+ * CUDA error. Shared-memory accesses and the warp kernels' staging copies are
+ * not checked. */
+int cbk_cuda_check_status(unsigned long long *count, int *first_i, int *first_j, int reset);
+
 /* Calibration, no reference counterpart: the measured fused multiply-add
  * rate of the current device in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1)
  * or FP32 (fp64 = 0), from a ~10 ms synthetic kernel -- the denominator of the

@@ -242,3 +242,17 @@ def test_noalloc_entry_validates_before_any_device_work():
     assert f(b"C", b"L", 0, 1, None, 1, None, 1, V, 10 ** 6, 10, None, None, None) == 0
     assert "too large" in cbk_gb300.status_string(900)
     assert "capturing" in cbk_gb300.status_string(901)
+
+
+def test_normal_build_reports_no_checking():
+    """cbk_cuda_check_status in the normal build: -1 (nothing is checked),
+    count 0, no device work."""
+    import ctypes
+
+    import cbk_gb300
+    f = cbk_gb300.lib().cbk_cuda_check_status
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_int),
+                  ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    count = ctypes.c_ulonglong(7)
+    assert f(ctypes.byref(count), None, None, 0) == -1 and count.value == 0
