@@ -1025,6 +1025,12 @@ def config_lines(names, args, cbk, dev, with_cpu=True):
                 for b in bks:
                     b["a"].copy_(b["a0"])
                     b["b"].copy_(b["b0"])
+            # the persistent grid from the library's autotuner (untimed; the
+            # graph bakes the launch in at capture)
+            tuned = None
+            if not args.no_tune:
+                info, tuned = cbk.autotune("sysvnp_bucketed", "d", 48, 48, nrhs, 1 << 17)
+                assert info == 0, info
             work = torch.empty(cbk.BUCKETED_LWORK, dtype=torch.uint8, device=dev)
             tup = [(b["n"], b["nm"], V, b["a"], b["n"], b["b"], b["n"]) for b in bks]
             graph = cbk.BucketedGraph("C", "L", nrhs, tup, work)
@@ -1044,6 +1050,9 @@ def config_lines(names, args, cbk, dev, with_cpu=True):
                         per_size_launches={"value": total / (tp * 1e-3), "ms_per_step": tp,
                                            "launches": len(bks)},
                         speedup_graph_vs_per_size=tp / tg,
+                        launch_shape=({"variant": tuned["variant"],
+                                       "grid": "one wave of warps halved 'variant' times"}
+                                      if tuned else "built-in (--no-tune)"),
                         roofline=roof(flops, nbytes, tg, "k_bucketed<double,true>"),
                         gpu_launches=args.steps)
             line["config"]["workload"] = ("dsysvnp_compact, 1048576 matrices, n uniform in "

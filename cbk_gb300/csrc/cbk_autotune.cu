@@ -227,6 +227,104 @@ int autotune(const Spec &sp, int m, int n, int nrhs, int nm, int only_V,
     return 0;
 }
 
+// The bucketed launch: a synthetic uneven batch -- orders from 4 (or 1) up
+// to n, nm matrices split evenly, each bucket uniform in [-1, 1) with the
+// diagonal raised by 2 k (diagonally dominant: both LDL^T without pivoting
+// and Cholesky apply) -- timed at every grid variant (the persistent warps
+// per SM halved 0 .. 3 times); the winner is stored at the largest order,
+// the key the launch reads.
+template <typename T>
+int autotune_bucketed(int routine, bool ldlt, int n, int nrhs, int nm, int only_V,
+                      const cbk_cuda_tune_result &old, cbk_cuda_tune_result *out)
+{
+    constexpr int ds = sizeof(T);
+    const int V = only_V ? only_V : 32;
+    const int lo = std::max(1, std::min(4, n));
+    int nb = n - lo + 1;
+    if (nb > CBK_CUDA_MAX_BUCKETS) nb = CBK_CUDA_MAX_BUCKETS;
+    const int per = std::max(32, nm / nb);
+    int ns[CBK_CUDA_MAX_BUCKETS], nms[CBK_CUDA_MAX_BUCKETS], Vs[CBK_CUDA_MAX_BUCKETS];
+    int lda[CBK_CUDA_MAX_BUCKETS], ldb[CBK_CUDA_MAX_BUCKETS];
+    T *a[CBK_CUDA_MAX_BUCKETS] = {}, *a0[CBK_CUDA_MAX_BUCKETS] = {};
+    T *b[CBK_CUDA_MAX_BUCKETS] = {}, *b0[CBK_CUDA_MAX_BUCKETS] = {};
+    size_t sa[CBK_CUDA_MAX_BUCKETS], sb[CBK_CUDA_MAX_BUCKETS];
+    void *work = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (!err) err = cudaEventCreate(&e0);
+    if (!err) err = cudaEventCreate(&e1);
+    if (!err) err = cudaMalloc(&work, CBK_CUDA_BUCKETED_LWORK);
+    for (int k = 0; k < nb && !err; ++k) {
+        // orders spread over lo .. n when there are more than the bucket limit
+        const int ord = nb == n - lo + 1 ? lo + k : lo + (int)((long)k * (n - lo) / (nb - 1));
+        ns[k] = ord;
+        nms[k] = per;
+        Vs[k] = V;
+        lda[k] = ord;
+        ldb[k] = ord;
+        const long lanes = ((long)per + V - 1) / V * V;
+        sa[k] = (size_t)lanes * ord * ord;
+        sb[k] = (size_t)lanes * ord * std::max(nrhs, 1);
+        if ((err = cudaMalloc(&a[k], sa[k] * ds)) || (err = cudaMalloc(&a0[k], sa[k] * ds)) ||
+            (err = cudaMalloc(&b[k], sb[k] * ds)) || (err = cudaMalloc(&b0[k], sb[k] * ds)))
+            break;
+        k_fill_uniform<T><<<256, 256, 0, s>>>(a0[k], (long)sa[k], 0x5EEDull + k);
+        k_fill_uniform<T><<<256, 256, 0, s>>>(b0[k], (long)sb[k], 0xB0Bull + k);
+        k_shift_diag<T><<<(unsigned)((lanes + 255) / 256), 256, 0, s>>>(a0[k], ord, V, lanes,
+                                                                        T(2 * ord));
+        err = cudaGetLastError();
+    }
+    float best = FLT_MAX;
+    int best_v = 0;
+    for (int v = 0; v < MAX_VARIANTS && !err; ++v) {
+        set_variant(routine, n, ds, v);
+        float vbest = FLT_MAX;
+        for (int rep = 0; rep < 4 && !err; ++rep) {
+            for (int k = 0; k < nb && !err; ++k)
+                if ((err = cudaMemcpyAsync(a[k], a0[k], sa[k] * ds, cudaMemcpyDeviceToDevice, s)) ||
+                    (err = cudaMemcpyAsync(b[k], b0[k], sb[k] * ds, cudaMemcpyDeviceToDevice, s)))
+                    break;
+            if (err || (err = cudaEventRecord(e0, s)) ||
+                (err = launch_bucketed<T>(ldlt, false, false, nrhs, nb, ns, nms, Vs, a, lda, b, ldb,
+                                          work, s)) ||
+                (err = cudaEventRecord(e1, s)) || (err = cudaEventSynchronize(e1)))
+                break;
+            float ms = 0.f;
+            if ((err = cudaEventElapsedTime(&ms, e0, e1))) break;
+            if (rep > 0) vbest = std::min(vbest, ms); // the first run warms up
+        }
+        if (!err && vbest < best) {
+            best = vbest;
+            best_v = v;
+        }
+    }
+    if (s) cudaStreamSynchronize(s);
+    for (int k = 0; k < nb; ++k) {
+        cudaFree(a[k]);
+        cudaFree(a0[k]);
+        cudaFree(b[k]);
+        cudaFree(b0[k]);
+    }
+    cudaFree(work);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (err) {
+        set_variant(routine, n, ds, old.variant);
+        return CBK_CUDA_ERROR_BASE + (int)err;
+    }
+    set_variant(routine, n, ds, best_v);
+    set_vlen(routine, n, ds, V);
+    if (out) {
+        out->threads = 0;
+        out->variant = best_v;
+        out->vlen = V;
+        out->ms = best;
+    }
+    return 0;
+}
+
 } // namespace
 
 } // namespace cbkcuda
@@ -249,6 +347,13 @@ int autotune_entry(const char *routine, char prec, int m, int n, int nrhs, int n
     if (nrhs < (rhs ? 1 : 0)) return -5;
     if (nm < 1) return -6;
     if (r == R_POSV_REFINED && prec != 'd') return -2;
+    if (r == R_SYSVNP_BUCKETED || r == R_POSV_BUCKETED) {
+        cbk_cuda_tune_result old{};
+        cbk_cuda_tune_get(routine, prec, n, &old);
+        const bool ldlt = r == R_SYSVNP_BUCKETED;
+        return prec == 'd' ? autotune_bucketed<double>(r, ldlt, n, nrhs, nm, only_V, old, out)
+                           : autotune_bucketed<float>(r, ldlt, n, nrhs, nm, only_V, old, out);
+    }
     Spec sp{r, FACTOR, false, false, n};
     switch (r) {
     case R_POTRF: sp = {r, FACTOR, false, true, n}; break;

@@ -113,8 +113,14 @@ cudaError_t launch_bucketed(bool ldlt, bool row, bool up, int nrhs, int nbuckets
     auto *counter = static_cast<unsigned long long *>(work);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    const int warps = ldlt ? resident_warps<T, true>() : resident_warps<T, false>();
-    const long want = std::min<long>(items, warps);
+    // the persistent grid: one wave of warps, or that halved `variant` times
+    // (fewer matrices in flight: a smaller working set in the L2 cache for the
+    // large orders, against less latency hiding); the variant is tuned per
+    // largest order
+    const int variant = variant_for(ldlt ? R_SYSVNP_BUCKETED : R_POSV_BUCKETED, tab.n[0],
+                                    (int)sizeof(T));
+    const int warps = (ldlt ? resident_warps<T, true>() : resident_warps<T, false>()) >> variant;
+    const long want = std::min<long>(items, std::max(warps, 4));
     const unsigned blocks = (unsigned)((want + 3) / 4);
     if (ldlt)
         k_bucketed<T, true><<<blocks, 128, 0, s>>>(tab, row, up, nrhs, counter);

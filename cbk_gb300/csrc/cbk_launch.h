@@ -16,8 +16,11 @@ namespace cbkcuda {
 int threads_for(int routine, int n, int dsize);
 void set_threads(int routine, int n, int dsize, int threads);
 
-// Compiled shape of a kernel that has several (0 = the built-in default).
-constexpr int MAX_VARIANTS = 2;
+// Compiled shape of a kernel that has several (0 = the built-in default):
+// 0 / 1 for the warp-per-matrix refined solve's register caps, the refined
+// solve's and least squares' kernel choice; 0 .. 3 for the bucketed launch
+// (the persistent grid's warps per SM halved `variant` times).
+constexpr int MAX_VARIANTS = 4;
 int variant_for(int routine, int n, int dsize);
 void set_variant(int routine, int n, int dsize, int variant);
 // the interleave width measured fastest (0: untuned)
@@ -31,7 +34,7 @@ int tune_slots();
 enum Routine {
     R_POTRF = 0, R_SYTRFNP, R_POTRS, R_POSV, R_SYTRSNP, R_SYSVNP, R_TRSM, R_GEQRF, R_ORMQR,
     R_ORGQR, R_GELS, R_ZERO, R_PACK, R_UNPACK, R_POSV_REFINED, R_GELS_REFINED, R_SYSVNP_BUCKETED,
-    R_COUNT
+    R_POSV_BUCKETED, R_COUNT
 };
 
 // every group of a rows x cols batch := 0

@@ -133,7 +133,8 @@ constexpr Name NAMES[] = {
     {"posv", R_POSV},     {"sytrsnp", R_SYTRSNP}, {"sysvnp", R_SYSVNP},
     {"trsm", R_TRSM},     {"geqrf", R_GEQRF},     {"ormqr", R_ORMQR},
     {"orgqr", R_ORGQR},   {"gels", R_GELS},       {"posv_refined", R_POSV_REFINED},
-    {"gels_refined", R_GELS_REFINED},
+    {"gels_refined", R_GELS_REFINED}, {"sysvnp_bucketed", R_SYSVNP_BUCKETED},
+    {"posv_bucketed", R_POSV_BUCKETED},
 };
 
 } // namespace

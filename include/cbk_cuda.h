@@ -443,21 +443,27 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
  * (advice for the caller's packing; a batch's width is the caller's). Entry
  * 0 means the built-in choice. Launch shapes never change results.
  * routine: "potrf", "sytrfnp", "potrs", "posv", "sytrsnp", "sysvnp", "trsm",
- * "geqrf", "ormqr", "orgqr", "gels", "posv_refined" or "gels_refined"; prec
+ * "geqrf", "ormqr", "orgqr", "gels", "posv_refined", "gels_refined",
+ * "sysvnp_bucketed" or "posv_bucketed"; prec
  * 'd' or 's' ('d' only for the refined solves); the order is n, except m for
  * the QR routines. "gels_refined" has one entry, set by cbk_cuda_tune_set
  * (not autotuned): variant 0 runs one warp per matrix where that kernel is
  * compiled (m <= 64, n = 8 or 16), variant 1 one lane per matrix.
+ * "sysvnp_bucketed" / "posv_bucketed" (keyed by the largest order of the
+ * launch): variant v runs the persistent grid with one wave of warps halved
+ * v times (0 .. 3) -- fewer matrices in flight keep the large orders' working
+ * set in the L2 cache, against less latency hiding.
  *
  * cbk_cuda_autotune times the routine on a synthetic batch of nm matrices
  * (m x n for the QR routines, m >= n; n x n otherwise; nrhs right-hand
- * sides) for every candidate shape at widths 32, 64 and 128, best of three
- * CUDA-event timings each, and stores the winner. It allocates and
+ * sides; for the bucketed launches nm matrices spread over the orders 4 .. n,
+ * at width 32) for every candidate shape at widths 32, 64 and 128, best of
+ * three CUDA-event timings each, and stores the winner. It allocates and
  * synchronises the device (not for use inside a stream capture). Returns 0,
  * -1 routine, -2 prec, -3 m, -4 n, -5 nrhs, -6 nm, or CBK_CUDA_ERROR_BASE + a
  * CUDA error (the table entry then keeps the built-in choice).
  * cbk_cuda_tune_set / _get write / read one entry (set: threads 0 or a
- * power of two 32 .. 512, variant 0 or 1, vlen 0 or a multiple of 32 up to
+ * power of two 32 .. 512, variant 0 .. 3, vlen 0 or a multiple of 32 up to
  * 1024; -j for the first illegal argument). cbk_cuda_tune_save writes every
  * non-default entry as text ("routine prec n threads variant vlen" lines);
  * cbk_cuda_tune_load reads such a file and returns the number of entries, -1

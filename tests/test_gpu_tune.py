@@ -68,3 +68,33 @@ def test_launch_shape_never_changes_results(tune, n, cuda):
         outs.append(_solve(tune, A, B, 32, refined=True))
     for o in outs[1:]:
         assert all(np.array_equal(x, y) for x, y in zip(outs[0], o))
+
+
+@pytest.mark.parametrize("routine", ["sysvnp_bucketed", "posv_bucketed"])
+def test_bucketed_grid_is_tuned_and_never_changes_results(tune, routine, cuda):
+    """The bucketed launch's persistent grid (variant v: one wave of warps
+    halved v times) is measured and stored at the largest order; every
+    variant gives the same bits."""
+    import torch
+    info, r = tune.autotune(routine, "d", 24, 24, 2, 4096)
+    assert info == 0 and r["variant"] in (0, 1, 2, 3) and r["threads"] == 0 and r["ms"] > 0
+    assert tune.tune_get(routine, "d", 24)[1]["variant"] == r["variant"]
+    rng = np.random.default_rng(5)
+    V, bks, host = 32, [], []
+    for n, nm in ((24, 300), (13, 500), (4, 900)):
+        A = C.gen_sym_ldlt(rng, nm, n, np.float64) if routine.startswith("sysvnp") else \
+            C.gen_spd(rng, nm, n, np.float64)
+        host.append((n, nm, O.pack(A, V), O.pack(rng.standard_normal((nm, n, 2)), V,
+                                                  pad_diag=0.0)))
+    outs = []
+    for v in (0, 1, 2, 3):
+        assert tune.tune_set(routine, "d", 24, variant=v) == 0
+        dev = [(n, nm, torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+               for n, nm, a, b in host]
+        bks = [(n, nm, V, a, n, b, n) for n, nm, a, b in dev]
+        assert tune.bucketed_compact(routine.split("_")[0], "d", "C", "L", 2, bks) == 0
+        torch.cuda.synchronize()
+        outs.append([(a.cpu().numpy(), b.cpu().numpy()) for _, _, a, b in dev])
+    for o in outs[1:]:
+        assert all(np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
+                   for x, y in zip(outs[0], o))

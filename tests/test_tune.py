@@ -29,6 +29,9 @@ def test_set_get_reset(tune):
     assert tune.tune_set("gels_refined", "d", 16, variant=1) == 0
     assert tune.tune_get("gels_refined", "d", 16)[1]["variant"] == 1
     assert tune.tune_get("gels_refined", "d", 8)[1]["variant"] == 0
+    assert tune.tune_set("sysvnp_bucketed", "d", 48, variant=3) == 0
+    assert tune.tune_get("sysvnp_bucketed", "d", 48)[1]["variant"] == 3
+    assert tune.tune_get("posv_bucketed", "d", 48)[1]["variant"] == 0
     # orders past 64 share one entry
     assert tune.tune_set("geqrf", "s", 100, threads=64) == 0
     assert tune.tune_get("geqrf", "s", 300)[1]["threads"] == 64
@@ -41,7 +44,7 @@ def test_argument_checks(tune):
     assert tune.tune_set("posv", "z", 8) == -2
     assert tune.tune_set("posv", "d", -1) == -3
     assert tune.tune_set("posv", "d", 8, threads=96) == -4
-    assert tune.tune_set("posv", "d", 8, variant=2) == -5
+    assert tune.tune_set("posv", "d", 8, variant=4) == -5
     assert tune.tune_set("posv", "d", 8, vlen=48) == -6
     assert tune.tune_get("nope", "d", 8)[0] == -1
     # autotune validates before touching the device
