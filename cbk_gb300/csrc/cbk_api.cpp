@@ -65,6 +65,19 @@ inline int cuda_status(cudaError_t e)
     return e == cudaSuccess ? 0 : CBK_CUDA_ERROR_BASE + (int)e;
 }
 
+// The host-pointer layer runs a routine's checks and quick returns first
+// without its launch (a dry run): every routine below returns 0 at the point
+// where it would launch, and records that it would have.
+thread_local bool tl_dry = false;
+thread_local bool tl_would_launch = false;
+
+inline bool dry_stop()
+{
+    if (!tl_dry) return false;
+    tl_would_launch = true;
+    return true;
+}
+
 template <typename T>
 int geqrf(char layout, int m, int n, T *ap, int ldap, T *taup, int V, int nm, cudaStream_t s)
 {
@@ -76,6 +89,7 @@ int geqrf(char layout, int m, int n, T *ap, int ldap, T *taup, int V, int nm, cu
     if (!vlen_ok(V)) return -7;
     if (nm < 0) return -8;
     if (m == 0 || n == 0 || nm == 0) return 0;
+    if (dry_stop()) return 0;
     return cuda_status(launch_geqrf<T>(row, m, n, ap, ldap, taup, V, nm, s));
 }
 
@@ -97,6 +111,7 @@ int ormqr(char layout, char side, char trans, int m, int n, int k, const T *ap, 
     if (!vlen_ok(V)) return -12;
     if (nm < 0) return -13;
     if (m == 0 || n == 0 || k == 0 || nm == 0) return 0;
+    if (dry_stop()) return 0;
     return cuda_status(launch_ormqr<T>(left, row, opt(trans, 'T'), m, n, k, ap, ldap, taup, cp,
                                        ldcp, V, nm, s));
 }
@@ -115,6 +130,7 @@ int orgqr(char layout, int m, int n, int k, T *ap, int ldap, const T *taup, int 
     if (nm < 0) return -9;
     // k == 0 is not empty: Q = I(:, 0:n-1) is still written
     if (m == 0 || n == 0 || nm == 0) return 0;
+    if (dry_stop()) return 0;
     return cuda_status(launch_orgqr<T>(row, m, n, k, ap, ldap, taup, V, nm, s));
 }
 
@@ -131,6 +147,7 @@ int factor(bool ldlt, char layout, char uplo, int n, T *ap, int ldap, int V, int
     if (!vlen_ok(V)) return -6;
     if (nm < 0) return -7;
     if (n == 0 || nm == 0) return 0;
+    if (dry_stop()) return 0;
     return cuda_status(launch_factor<T>(ldlt, row, up, n, ap, ldap, V, nm, s));
 }
 
@@ -164,8 +181,10 @@ int sym_solve(bool ldlt, bool fused, char layout, char uplo, int n, int nrhs, T 
         // the solve alone has nothing to do; the fused driver still factors
         // (LAPACK ?posv / ?sysv), never referencing bp
         if (!fused) return 0;
+        if (dry_stop()) return 0;
         return cuda_status(launch_factor<T>(ldlt, row, up, n, ap, ldap, V, nm, s));
     }
+    if (dry_stop()) return 0;
     return cuda_status(
         launch_sym_solve<T>(ldlt, fused, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, s));
 }
@@ -193,6 +212,7 @@ int trsm(char layout, char side, char uplo, char transa, char diag, int m, int n
     if (!vlen_ok(V)) return -13;
     if (nm < 0) return -14;
     if (m == 0 || n == 0 || nm == 0) return 0;
+    if (dry_stop()) return 0;
     if (alpha == T(0)) return cuda_status(launch_zero<T>(row, m, n, bp, ldbp, V, nm, s));
     return cuda_status(
         launch_trsm<T>(left, up, row, tran, unit, m, n, alpha, ap, ldap, bp, ldbp, V, nm, s));
@@ -215,6 +235,7 @@ int gels(char layout, char trans, int m, int n, int nrhs, T *ap, int ldap, T *bp
     if (nm < 0) return -12;
     if (nrhs == 0 || nm == 0 || mx == 0) return 0;
     const bool tran = opt(trans, 'T') || opt(trans, 'C');
+    if (dry_stop()) return 0;
     return cuda_status(
         launch_gels<T>(row, tran, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, s));
 }
@@ -385,6 +406,220 @@ int bucketed(bool ldlt, char layout, char uplo, int nrhs, int nbuckets, const Bu
 inline cudaStream_t S(cbk_stream_t s)
 {
     return reinterpret_cast<cudaStream_t>(s);
+}
+
+// ---------------------------------------------------------------------
+// The host-pointer layer: the reference's calling convention (every array
+// on the host) over the device routines above, through a caller-provided
+// device workspace
+// ---------------------------------------------------------------------
+
+struct HostArray {
+    void *host;
+    size_t bytes;
+    bool in, out;
+};
+
+inline size_t align256(size_t b)
+{
+    return (b + 255) & ~(size_t)255;
+}
+
+// bytes of a compact batch of nm rows x cols matrices, leading dimension ld
+inline size_t compact_bytes(bool row, int ld, int rows, int cols, int V, int nm, size_t es)
+{
+    if (rows <= 0 || cols <= 0 || nm <= 0) return 0;
+    const size_t ng = ((size_t)nm + V - 1) / V;
+    return ng * (size_t)ld * (size_t)(row ? rows : cols) * (size_t)V * es;
+}
+
+// a routine's checks and quick returns, without its launch: its code, and in
+// `launch` whether it has device work
+template <typename F> int dry_run(F &&call, bool &launch)
+{
+    tl_dry = true;
+    tl_would_launch = false;
+    const int info = call();
+    tl_dry = false;
+    launch = tl_would_launch;
+    return info;
+}
+
+// nothing to copy (an illegal argument or a quick return): a size query
+// answers 0
+inline int host_quick(int info, long long *lwork)
+{
+    if (info == 0 && lwork && *lwork < 0) *lwork = 0;
+    return info;
+}
+
+// The arrays into the workspace (256-byte aligned, in order), the routine on
+// them, the outputs back, the stream synchronised. wpos: the position of
+// the dwork argument (-wpos: dwork null or *lwork too small; -(wpos + 1):
+// lwork null). *lwork < 0 asks for the size instead.
+template <typename F>
+int host_run(int wpos, const HostArray *arr, int na, void *dwork, long long *lwork, cudaStream_t s,
+             F &&run)
+{
+    size_t off[4], need = 0;
+    for (int i = 0; i < na; ++i) {
+        off[i] = need;
+        need += align256(arr[i].bytes);
+    }
+    if (!lwork) return -(wpos + 1);
+    if (*lwork < 0) {
+        *lwork = (long long)need;
+        return 0;
+    }
+    if ((size_t)*lwork < need || (need > 0 && !dwork)) return -wpos;
+    char *d = static_cast<char *>(dwork);
+    void *dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < na && e == cudaSuccess; ++i) {
+        dev[i] = arr[i].bytes ? d + off[i] : nullptr;
+        if (arr[i].in && arr[i].bytes)
+            e = cudaMemcpyAsync(dev[i], arr[i].host, arr[i].bytes, cudaMemcpyHostToDevice, s);
+    }
+    int info = e == cudaSuccess ? run(dev) : cuda_status(e);
+    if (info == 0)
+        for (int i = 0; i < na && e == cudaSuccess; ++i)
+            if (arr[i].out && arr[i].bytes)
+                e = cudaMemcpyAsync(arr[i].host, dev[i], arr[i].bytes, cudaMemcpyDeviceToHost, s);
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    if (info != 0) return info;
+    if (e != cudaSuccess) return cuda_status(e);
+    return cuda_status(e2);
+}
+
+template <typename T>
+int host_geqrf(char layout, int m, int n, T *ap, int ldap, T *taup, int V, int nm, void *dw,
+               long long *lw, cudaStream_t s)
+{
+    bool go;
+    const int info = dry_run([&] { return geqrf<T>(layout, m, n, ap, ldap, taup, V, nm, s); }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const int k = m < n ? m : n;
+    const HostArray a[2] = {{ap, compact_bytes(row, ldap, m, n, V, nm, sizeof(T)), true, true},
+                            {taup, compact_bytes(false, k, k, 1, V, nm, sizeof(T)), false, true}};
+    return host_run(9, a, 2, dw, lw, s, [&](void **d) {
+        return geqrf<T>(layout, m, n, (T *)d[0], ldap, (T *)d[1], V, nm, s);
+    });
+}
+
+template <typename T>
+int host_ormqr(char layout, char side, char trans, int m, int n, int k, const T *ap, int ldap,
+               const T *taup, T *cp, int ldcp, int V, int nm, void *dw, long long *lw,
+               cudaStream_t s)
+{
+    bool go;
+    const int info = dry_run(
+        [&] { return ormqr<T>(layout, side, trans, m, n, k, ap, ldap, taup, cp, ldcp, V, nm, s); },
+        go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const int nq = opt(side, 'L') ? m : n;
+    const HostArray a[3] = {
+        {const_cast<T *>(ap), compact_bytes(row, ldap, nq, k, V, nm, sizeof(T)), true, false},
+        {const_cast<T *>(taup), compact_bytes(false, k, k, 1, V, nm, sizeof(T)), true, false},
+        {cp, compact_bytes(row, ldcp, m, n, V, nm, sizeof(T)), true, true}};
+    return host_run(14, a, 3, dw, lw, s, [&](void **d) {
+        return ormqr<T>(layout, side, trans, m, n, k, (const T *)d[0], ldap, (const T *)d[1],
+                        (T *)d[2], ldcp, V, nm, s);
+    });
+}
+
+template <typename T>
+int host_orgqr(char layout, int m, int n, int k, T *ap, int ldap, const T *taup, int V, int nm,
+               void *dw, long long *lw, cudaStream_t s)
+{
+    bool go;
+    const int info =
+        dry_run([&] { return orgqr<T>(layout, m, n, k, ap, ldap, taup, V, nm, s); }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const HostArray a[2] = {
+        {ap, compact_bytes(row, ldap, m, n, V, nm, sizeof(T)), true, true},
+        {const_cast<T *>(taup), compact_bytes(false, k, k, 1, V, nm, sizeof(T)), true, false}};
+    return host_run(10, a, 2, dw, lw, s, [&](void **d) {
+        return orgqr<T>(layout, m, n, k, (T *)d[0], ldap, (const T *)d[1], V, nm, s);
+    });
+}
+
+template <typename T>
+int host_factor(bool ldlt, char layout, char uplo, int n, T *ap, int ldap, int V, int nm,
+                void *dw, long long *lw, cudaStream_t s)
+{
+    bool go;
+    const int info =
+        dry_run([&] { return factor<T>(ldlt, layout, uplo, n, ap, ldap, V, nm, s); }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const HostArray a[1] = {
+        {ap, compact_bytes(opt(layout, 'R'), ldap, n, n, V, nm, sizeof(T)), true, true}};
+    return host_run(8, a, 1, dw, lw, s, [&](void **d) {
+        return factor<T>(ldlt, layout, uplo, n, (T *)d[0], ldap, V, nm, s);
+    });
+}
+
+// ?potrs / ?sytrsnp (fused = false: A read only) and ?posv / ?sysvnp
+template <typename T>
+int host_sym_solve(bool ldlt, bool fused, char layout, char uplo, int n, int nrhs, T *ap,
+                   int ldap, T *bp, int ldbp, int V, int nm, void *dw, long long *lw,
+                   cudaStream_t s)
+{
+    bool go;
+    const int info = dry_run([&] {
+        return sym_solve<T>(ldlt, fused, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm, s);
+    }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const HostArray a[2] = {{ap, compact_bytes(row, ldap, n, n, V, nm, sizeof(T)), true, fused},
+                            {bp, compact_bytes(row, ldbp, n, nrhs, V, nm, sizeof(T)), true, true}};
+    return host_run(11, a, 2, dw, lw, s, [&](void **d) {
+        return sym_solve<T>(ldlt, fused, layout, uplo, n, nrhs, (T *)d[0], ldap, (T *)d[1], ldbp,
+                            V, nm, s);
+    });
+}
+
+template <typename T>
+int host_trsm(char layout, char side, char uplo, char transa, char diag, int m, int n, T alpha,
+              const T *ap, int ldap, T *bp, int ldbp, int V, int nm, void *dw, long long *lw,
+              cudaStream_t s)
+{
+    bool go;
+    const int info = dry_run([&] {
+        return trsm<T>(layout, side, uplo, transa, diag, m, n, alpha, ap, ldap, bp, ldbp, V, nm,
+                       s);
+    }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const int sdim = opt(side, 'L') ? m : n;
+    const size_t abytes = alpha == T(0) ? 0 : compact_bytes(row, ldap, sdim, sdim, V, nm, sizeof(T));
+    const HostArray a[2] = {{const_cast<T *>(ap), abytes, true, false},
+                            {bp, compact_bytes(row, ldbp, m, n, V, nm, sizeof(T)), true, true}};
+    return host_run(15, a, 2, dw, lw, s, [&](void **d) {
+        return trsm<T>(layout, side, uplo, transa, diag, m, n, alpha, (const T *)d[0], ldap,
+                       (T *)d[1], ldbp, V, nm, s);
+    });
+}
+
+template <typename T>
+int host_gels(char layout, char trans, int m, int n, int nrhs, T *ap, int ldap, T *bp, int ldbp,
+              T *taup, int V, int nm, void *dw, long long *lw, cudaStream_t s)
+{
+    bool go;
+    const int info = dry_run(
+        [&] { return gels<T>(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, s); }, go);
+    if (info != 0 || !go) return host_quick(info, lw);
+    const bool row = opt(layout, 'R');
+    const int k = m < n ? m : n, mx = m > n ? m : n;
+    const HostArray a[3] = {{ap, compact_bytes(row, ldap, m, n, V, nm, sizeof(T)), true, true},
+                            {bp, compact_bytes(row, ldbp, mx, nrhs, V, nm, sizeof(T)), true, true},
+                            {taup, compact_bytes(false, k, k, 1, V, nm, sizeof(T)), false, true}};
+    return host_run(13, a, 3, dw, lw, s, [&](void **d) {
+        return gels<T>(layout, trans, m, n, nrhs, (T *)d[0], ldap, (T *)d[1], ldbp, (T *)d[2], V,
+                       nm, s);
+    });
 }
 
 } // namespace
@@ -765,5 +1000,87 @@ CBK_CUDA_ENTRY_POINTS(double, d)
 CBK_CUDA_ENTRY_POINTS(float, s)
 
 #undef CBK_CUDA_ENTRY_POINTS
+
+
+// The host-pointer forms, one per routine and scalar type.
+#define CBK_CUDA_HOST_ENTRY_POINTS(T, p)                                                          \
+    int cbk_cuda_host_##p##geqrf_compact(char layout, int m, int n, T *ap, int ldap, T *taup,    \
+                                         int V, int nm, void *dwork, long long *lwork,            \
+                                         cbk_stream_t st)                                         \
+    {                                                                                             \
+        return host_geqrf<T>(layout, m, n, ap, ldap, taup, V, nm, dwork, lwork, S(st));           \
+    }                                                                                             \
+    int cbk_cuda_host_##p##ormqr_compact(char layout, char side, char trans, int m, int n, int k, \
+                                         const T *ap, int ldap, const T *taup, T *cp, int ldcp,   \
+                                         int V, int nm, void *dwork, long long *lwork,            \
+                                         cbk_stream_t st)                                         \
+    {                                                                                             \
+        return host_ormqr<T>(layout, side, trans, m, n, k, ap, ldap, taup, cp, ldcp, V, nm,       \
+                             dwork, lwork, S(st));                                                \
+    }                                                                                             \
+    int cbk_cuda_host_##p##orgqr_compact(char layout, int m, int n, int k, T *ap, int ldap,       \
+                                         const T *taup, int V, int nm, void *dwork,               \
+                                         long long *lwork, cbk_stream_t st)                       \
+    {                                                                                             \
+        return host_orgqr<T>(layout, m, n, k, ap, ldap, taup, V, nm, dwork, lwork, S(st));        \
+    }                                                                                             \
+    int cbk_cuda_host_##p##potrf_compact(char layout, char uplo, int n, T *ap, int ldap, int V,   \
+                                         int nm, void *dwork, long long *lwork, cbk_stream_t st)  \
+    {                                                                                             \
+        return host_factor<T>(false, layout, uplo, n, ap, ldap, V, nm, dwork, lwork, S(st));      \
+    }                                                                                             \
+    int cbk_cuda_host_##p##sytrfnp_compact(char layout, char uplo, int n, T *ap, int ldap, int V, \
+                                           int nm, void *dwork, long long *lwork,                 \
+                                           cbk_stream_t st)                                       \
+    {                                                                                             \
+        return host_factor<T>(true, layout, uplo, n, ap, ldap, V, nm, dwork, lwork, S(st));       \
+    }                                                                                             \
+    int cbk_cuda_host_##p##potrs_compact(char layout, char uplo, int n, int nrhs, const T *ap,    \
+                                         int ldap, T *bp, int ldbp, int V, int nm, void *dwork,   \
+                                         long long *lwork, cbk_stream_t st)                       \
+    {                                                                                             \
+        return host_sym_solve<T>(false, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap,  \
+                                 bp, ldbp, V, nm, dwork, lwork, S(st));                           \
+    }                                                                                             \
+    int cbk_cuda_host_##p##posv_compact(char layout, char uplo, int n, int nrhs, T *ap, int ldap, \
+                                        T *bp, int ldbp, int V, int nm, void *dwork,              \
+                                        long long *lwork, cbk_stream_t st)                        \
+    {                                                                                             \
+        return host_sym_solve<T>(false, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm,   \
+                                 dwork, lwork, S(st));                                            \
+    }                                                                                             \
+    int cbk_cuda_host_##p##sytrsnp_compact(char layout, char uplo, int n, int nrhs, const T *ap,  \
+                                           int ldap, T *bp, int ldbp, int V, int nm, void *dwork, \
+                                           long long *lwork, cbk_stream_t st)                     \
+    {                                                                                             \
+        return host_sym_solve<T>(true, false, layout, uplo, n, nrhs, const_cast<T *>(ap), ldap,   \
+                                 bp, ldbp, V, nm, dwork, lwork, S(st));                           \
+    }                                                                                             \
+    int cbk_cuda_host_##p##sysvnp_compact(char layout, char uplo, int n, int nrhs, T *ap,         \
+                                          int ldap, T *bp, int ldbp, int V, int nm, void *dwork,  \
+                                          long long *lwork, cbk_stream_t st)                      \
+    {                                                                                             \
+        return host_sym_solve<T>(true, true, layout, uplo, n, nrhs, ap, ldap, bp, ldbp, V, nm,    \
+                                 dwork, lwork, S(st));                                            \
+    }                                                                                             \
+    int cbk_cuda_host_##p##trsm_compact(char layout, char side, char uplo, char transa,          \
+                                        char diag, int m, int n, T alpha, const T *ap, int ldap,  \
+                                        T *bp, int ldbp, int V, int nm, void *dwork,              \
+                                        long long *lwork, cbk_stream_t st)                        \
+    {                                                                                             \
+        return host_trsm<T>(layout, side, uplo, transa, diag, m, n, alpha, ap, ldap, bp, ldbp, V, \
+                            nm, dwork, lwork, S(st));                                             \
+    }                                                                                             \
+    int cbk_cuda_host_##p##gels_compact(char layout, char trans, int m, int n, int nrhs, T *ap,   \
+                                        int ldap, T *bp, int ldbp, T *taup, int V, int nm,        \
+                                        void *dwork, long long *lwork, cbk_stream_t st)           \
+    {                                                                                             \
+        return host_gels<T>(layout, trans, m, n, nrhs, ap, ldap, bp, ldbp, taup, V, nm, dwork,    \
+                            lwork, S(st));                                                        \
+    }
+
+CBK_CUDA_HOST_ENTRY_POINTS(double, d)
+CBK_CUDA_HOST_ENTRY_POINTS(float, s)
+#undef CBK_CUDA_HOST_ENTRY_POINTS
 
 } // extern "C"

@@ -198,6 +198,63 @@ int cbk_cuda_sgels_compact_async(char layout, char trans, int m, int n, int nrhs
                                  int ldap, float *bp, int ldbp, float *taup, int V, int nm,
                                  cbk_stream_t stream);
 
+/* The same routines on HOST arrays: the reference's own calling convention
+ * (include/cbk.h:77-352, every array on the host; its MKL-style adapter,
+ * src/cbk_compat.cpp:252-333, is such a layer over the kernels too) over the
+ * device routines above. cbk_cuda_host_NAME_compact takes NAME's arguments
+ * unchanged -- host pointers, the same -j codes in the same order, the same
+ * quick returns, which touch no array and need no workspace -- plus:
+ *   dwork  device memory of at least *lwork bytes (the call never allocates);
+ *   lwork  in: the bytes of dwork, or a negative value to ask: the call then
+ *          checks the arguments, stores the bytes it needs in *lwork (0 when
+ *          there is nothing to compute) and returns, touching nothing else;
+ *   stream the stream the copies and kernels run on.
+ * The call copies the arrays the routine reads to dwork, runs it there,
+ * copies the arrays it writes back and synchronises the stream; the host
+ * arrays then hold exactly what NAME_compact_async leaves in device memory.
+ * Extra codes: -(k+1) dwork NULL or *lwork too small, -(k+2) lwork NULL,
+ * where k is NAME's argument count (geqrf 8, ormqr 13, orgqr 9, potrf and
+ * sytrfnp 7, potrs, posv, sytrsnp and sysvnp 10, trsm 14, gels 12). */
+#define CBK_CUDA_HOST_DECLS(T, p)                                                                  \
+    int cbk_cuda_host_##p##geqrf_compact(char layout, int m, int n, T *ap, int ldap, T *taup,     \
+                                         int V, int nm, void *dwork, long long *lwork,             \
+                                         cbk_stream_t stream);                                     \
+    int cbk_cuda_host_##p##ormqr_compact(char layout, char side, char trans, int m, int n, int k,  \
+                                         const T *ap, int ldap, const T *taup, T *cp, int ldcp,    \
+                                         int V, int nm, void *dwork, long long *lwork,             \
+                                         cbk_stream_t stream);                                     \
+    int cbk_cuda_host_##p##orgqr_compact(char layout, int m, int n, int k, T *ap, int ldap,        \
+                                         const T *taup, int V, int nm, void *dwork,                \
+                                         long long *lwork, cbk_stream_t stream);                   \
+    int cbk_cuda_host_##p##potrf_compact(char layout, char uplo, int n, T *ap, int ldap, int V,    \
+                                         int nm, void *dwork, long long *lwork,                    \
+                                         cbk_stream_t stream);                                     \
+    int cbk_cuda_host_##p##sytrfnp_compact(char layout, char uplo, int n, T *ap, int ldap, int V,  \
+                                           int nm, void *dwork, long long *lwork,                  \
+                                           cbk_stream_t stream);                                   \
+    int cbk_cuda_host_##p##potrs_compact(char layout, char uplo, int n, int nrhs, const T *ap,     \
+                                         int ldap, T *bp, int ldbp, int V, int nm, void *dwork,    \
+                                         long long *lwork, cbk_stream_t stream);                   \
+    int cbk_cuda_host_##p##posv_compact(char layout, char uplo, int n, int nrhs, T *ap, int ldap,  \
+                                        T *bp, int ldbp, int V, int nm, void *dwork,               \
+                                        long long *lwork, cbk_stream_t stream);                    \
+    int cbk_cuda_host_##p##sytrsnp_compact(char layout, char uplo, int n, int nrhs, const T *ap,   \
+                                           int ldap, T *bp, int ldbp, int V, int nm, void *dwork,  \
+                                           long long *lwork, cbk_stream_t stream);                 \
+    int cbk_cuda_host_##p##sysvnp_compact(char layout, char uplo, int n, int nrhs, T *ap,          \
+                                          int ldap, T *bp, int ldbp, int V, int nm, void *dwork,   \
+                                          long long *lwork, cbk_stream_t stream);                  \
+    int cbk_cuda_host_##p##trsm_compact(char layout, char side, char uplo, char transa,           \
+                                        char diag, int m, int n, T alpha, const T *ap, int ldap,   \
+                                        T *bp, int ldbp, int V, int nm, void *dwork,               \
+                                        long long *lwork, cbk_stream_t stream);                    \
+    int cbk_cuda_host_##p##gels_compact(char layout, char trans, int m, int n, int nrhs, T *ap,    \
+                                        int ldap, T *bp, int ldbp, T *taup, int V, int nm,         \
+                                        void *dwork, long long *lwork, cbk_stream_t stream);
+CBK_CUDA_HOST_DECLS(double, d)
+CBK_CUDA_HOST_DECLS(float, s)
+#undef CBK_CUDA_HOST_DECLS
+
 /* Dense batch <-> compact layout on the device. No reference entry point:
  * the device form of the reference tests' pack_compact / unpack_compact
  * (tests/test_compact_util.hpp:477-531) and of mkl_?gepack_compact.

@@ -23,6 +23,9 @@ def declared_functions():
             text = open(os.path.join(ROOT, "include", h)).read()
             text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
             names |= set(re.findall(r"\b(cbk_cuda_\w+)\s*\(", text))
+            # declarations written once per scalar type by a macro
+            for stem in re.findall(r"\b(cbk_cuda_\w+?)_##p##(\w+)\s*\(", text):
+                names |= {f"{stem[0]}_{p}{stem[1]}" for p in "ds"}
     return sorted(names)
 
 
@@ -256,3 +259,46 @@ def test_normal_build_reports_no_checking():
                   ctypes.POINTER(ctypes.c_int), ctypes.c_int]
     count = ctypes.c_ulonglong(7)
     assert f(ctypes.byref(count), None, None, 0) == -1 and count.value == 0
+
+
+def test_host_layer_argument_codes_and_quick_returns():
+    """The host-pointer layer returns every routine's -j codes and quick
+    returns before touching an array (null host pointers, no workspace), and
+    a size query of a quick return answers 0."""
+    import ctypes
+
+    import abi_tables
+    import host_layer as H
+    for routine, dtype, args, code in abi_tables.rows_with_codes():
+        lw = ctypes.c_longlong(-1)
+        assert H.call(dtype, routine, args, None, lw) == code, (routine, args, code)
+        if code == 0:
+            assert lw.value == 0, (routine, args)
+
+
+def test_host_layer_workspace_query_and_codes():
+    """Size query: the arrays the routine touches, each 256-byte aligned; then
+    -(k+1) for a missing or small workspace and -(k+2) for a null lwork (k the
+    routine's argument count) -- all before any device work."""
+    import ctypes
+
+    import host_layer as H
+    a = np.zeros(2 * 8 * 8 * 32)
+    b = np.zeros(2 * 8 * 32)
+    args = ["C", "L", 8, 1, a, 8, b, 8, 32, 64]
+    lw = ctypes.c_longlong(-1)
+    assert H.call(np.float64, "posv", args, None, lw) == 0
+    assert lw.value == 2 * 8 * 8 * 32 * 8 + 2 * 8 * 1 * 32 * 8
+    small = ctypes.c_longlong(lw.value - 1)
+    assert H.call(np.float64, "posv", args, 1 << 40, small) == -11
+    assert H.call(np.float64, "posv", args, None, ctypes.c_longlong(lw.value)) == -11
+    assert H.call(np.float64, "posv", args, None, None) == -12
+    # potrs reads A and writes B; trsm with alpha = 0 never reads A
+    lw = ctypes.c_longlong(-1)
+    assert H.call(np.float64, "trsm", ["C", "L", "U", "N", "N", 8, 2, 0.0, None, 8,
+                                       np.zeros(2 * 8 * 2 * 32), 8, 32, 64], None, lw) == 0
+    assert lw.value == 2 * 8 * 2 * 32 * 8
+    lw = ctypes.c_longlong(-1)  # gels 16 x 8: A, B and tau
+    assert H.call(np.float32, "gels", ["C", "N", 16, 8, 4, None, 16, None, 16, None, 32, 40],
+                  None, lw) == 0
+    assert lw.value == 2 * 16 * 8 * 32 * 4 + 2 * 16 * 4 * 32 * 4 + 2 * 8 * 32 * 4
