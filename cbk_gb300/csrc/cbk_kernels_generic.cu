@@ -64,17 +64,17 @@ __global__ void k_trsm(bool left, bool up, bool row, bool tran, bool unit, int m
                  lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, m, n));
 }
 
-template <typename T>
+template <typename T, bool WY>
 __global__ void k_geqrf(bool row, int m, int n, T *ap, int ldap, T *taup, int V, long ngroups,
                         size_t sa, size_t st)
 {
     Lane ln;
     if (!lane_of(ngroups, V, ln)) return;
-    geqrf_lane<T>(m, n, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, m, n),
+    geqrf_lane<T, WY>(m, n, lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, m, n),
                   taup + ln.g * st + ln.v, V);
 }
 
-template <typename T>
+template <typename T, bool WY>
 __global__ void k_ormqr(bool left, bool row, bool forward, int m, int n, int k, const T *ap,
                         int ldap, const T *taup, T *cp, int ldcp, int V, long ngroups, size_t sa,
                         size_t st, size_t sc)
@@ -85,7 +85,7 @@ __global__ void k_ormqr(bool left, bool row, bool forward, int m, int n, int k, 
         lv_make<T>(const_cast<T *>(ap) + ln.g * sa + ln.v, row, ldap, V, left ? m : n, k);
     LV<T> C = lv_make<T>(cp + ln.g * sc + ln.v, row, ldcp, V, m, n);
     if (!left) C = C.t();
-    ormqr_lane<T>(forward, left ? m : n, left ? n : m, k, A, taup + ln.g * st + ln.v, V, C);
+    ormqr_lane<T, WY>(forward, left ? m : n, left ? n : m, k, A, taup + ln.g * st + ln.v, V, C);
 }
 
 template <typename T>
@@ -98,7 +98,7 @@ __global__ void k_orgqr(bool row, int m, int n, int k, T *ap, int ldap, const T 
                   taup + ln.g * st + ln.v, V);
 }
 
-template <typename T>
+template <typename T, bool WY>
 __global__ void k_gels(bool row, bool tall, bool overdet, int p, int q, int nrhs, T *ap, int ldap,
                        T *bp, int ldbp, T *taup, int V, long ngroups, size_t sa, size_t sb,
                        size_t st)
@@ -107,7 +107,7 @@ __global__ void k_gels(bool row, bool tall, bool overdet, int p, int q, int nrhs
     if (!lane_of(ngroups, V, ln)) return;
     LV<T> A = lv_make<T>(ap + ln.g * sa + ln.v, row, ldap, V, tall ? p : q, tall ? q : p);
     if (!tall) A = A.t();
-    gels_lane<T>(overdet, p, q, nrhs, A, taup + ln.g * st + ln.v, V,
+    gels_lane<T, WY>(overdet, p, q, nrhs, A, taup + ln.g * st + ln.v, V,
                  lv_make<T>(bp + ln.g * sb + ln.v, row, ldbp, V, p, nrhs));
 }
 
@@ -185,8 +185,11 @@ cudaError_t launch_geqrf(bool row, int m, int n, T *ap, int ldap, T *taup, int V
     const long ng = groups_of(nm, V);
     const int k = m < n ? m : n;
     const int th = threads_for(R_GEQRF, m, sizeof(T));
-    k_geqrf<T><<<blocks_for(ng, V, th), th, 0, s>>>(row, m, n, ap, ldap, taup, V, ng,
-                                                    gstride(row, ldap, m, n, V), (size_t)k * V);
+    // the compact-WY kernel from WY_MMIN rows on (its extra registers would
+    // cost the one-at-a-time kernel occupancy)
+    auto kern = m >= WY_MMIN ? k_geqrf<T, true> : k_geqrf<T, false>;
+    kern<<<blocks_for(ng, V, th), th, 0, s>>>(row, m, n, ap, ldap, taup, V, ng,
+                                              gstride(row, ldap, m, n, V), (size_t)k * V);
     return cudaGetLastError();
 }
 
@@ -198,9 +201,10 @@ cudaError_t launch_ormqr(bool left, bool row, bool tran, int m, int n, int k, co
     const int len = left ? m : n;
     const bool forward = (left == tran);
     const int th = threads_for(R_ORMQR, len, sizeof(T));
-    k_ormqr<T><<<blocks_for(ng, V, th), th, 0, s>>>(left, row, forward, m, n, k, ap, ldap, taup, cp,
-                                                    ldcp, V, ng, gstride(row, ldap, len, k, V),
-                                                    (size_t)k * V, gstride(row, ldcp, m, n, V));
+    auto kern = len >= WY_MMIN ? k_ormqr<T, true> : k_ormqr<T, false>;
+    kern<<<blocks_for(ng, V, th), th, 0, s>>>(left, row, forward, m, n, k, ap, ldap, taup, cp, ldcp,
+                                              V, ng, gstride(row, ldap, len, k, V), (size_t)k * V,
+                                              gstride(row, ldcp, m, n, V));
     return cudaGetLastError();
 }
 
@@ -225,9 +229,10 @@ cudaError_t launch_gels(bool row, bool tran, int m, int n, int nrhs, T *ap, int 
     const bool overdet = (tall != tran);
     if (q == 0) return launch_zero<T>(row, p, nrhs, bp, ldbp, V, nm, s);
     const int th = threads_for(R_GELS, p, sizeof(T));
-    k_gels<T><<<blocks_for(ng, V, th), th, 0, s>>>(row, tall, overdet, p, q, nrhs, ap, ldap, bp,
-                                                   ldbp, taup, V, ng, gstride(row, ldap, m, n, V),
-                                                   gstride(row, ldbp, p, nrhs, V), (size_t)q * V);
+    auto kern = p >= WY_MMIN ? k_gels<T, true> : k_gels<T, false>;
+    kern<<<blocks_for(ng, V, th), th, 0, s>>>(row, tall, overdet, p, q, nrhs, ap, ldap, bp, ldbp,
+                                              taup, V, ng, gstride(row, ldap, m, n, V),
+                                              gstride(row, ldbp, p, nrhs, V), (size_t)q * V);
     return cudaGetLastError();
 }
 

@@ -68,6 +68,43 @@ def test_parity_benchmark_shapes(V, nm, cuda, oracle_lib):
     print(f"benchmark shapes V={V}: {len(cases)} cases, worst ratio / order = {worst:.2f} eps")
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("layout", ["C", "R"])
+def test_parity_blocked_qr(dtype, layout, cuda, oracle_lib):
+    """From 32 rows on the QR family applies its reflectors in compact-WY
+    blocks of four: geqrf (whole blocks and a ragged last one), ormqr from
+    both sides in both directions (forward and backward block order), gels
+    over- and under-determined, and orgqr on the blocked QR's reflectors --
+    against the oracle, which applies them one at a time."""
+    worst = 0.0
+    cases = []
+    seed = 8100
+    for mm, nn in ((40, 12), (64, 16), (33, 7), (48, 48)):
+        seed += 1
+        cases.append(C.make_case("geqrf", dtype, seed, 32, 37, layout, m=mm, n=nn,
+                                 ldpad=seed % 2))
+    for side in "LR":
+        for tr in "NT":
+            for (mm, nn, kk) in ((40, 5, 12), (36, 40, 9), (64, 8, 16)):
+                seed += 1
+                if kk > (mm if side == "L" else nn):
+                    continue
+                cases.append(C.make_case("ormqr", dtype, seed, 32, 37, layout, m=mm, n=nn, k=kk,
+                                         side=side, trans=tr, ldpad=seed % 2))
+    for tr in "NT":
+        for (mm, nn, nr) in ((64, 16, 8), (40, 13, 3), (16, 48, 2)):
+            seed += 1
+            cases.append(C.make_case("gels", dtype, seed, 32, 37, layout, m=mm, n=nn, nrhs=nr,
+                                     trans=tr, ldpad=seed % 2))
+    seed += 1
+    cases.append(C.make_case("orgqr", dtype, seed, 32, 37, layout, m=48, n=16, k=16))
+    for c in cases:
+        gi, g = G.run_gpu(c)
+        oi, o = C.run(oracle_lib, c)
+        worst = max(worst, _check(c, gi, g, oi, o))
+    print(f"blocked QR {layout}: {len(cases)} cases, worst ratio / order = {worst:.2f} eps")
+
+
 def test_parity_golden(cuda):
     worst = 0.0
     for cin, cout, info in make_golden.load():
