@@ -1025,11 +1025,13 @@ def config_lines(names, args, cbk, dev, with_cpu=True):
                 for b in bks:
                     b["a"].copy_(b["a0"])
                     b["b"].copy_(b["b0"])
-            # the persistent grid from the library's autotuner (untimed; the
-            # graph bakes the launch in at capture)
+            # the persistent grid from the library's autotuner on a batch of
+            # this workload's size (untimed; the graph bakes the launch in at
+            # capture). A smaller tuning batch misleads: at 2^17 matrices the
+            # halved grid can measure faster, at 2^20 it is 30 % slower.
             tuned = None
             if not args.no_tune:
-                info, tuned = cbk.autotune("sysvnp_bucketed", "d", 48, 48, nrhs, 1 << 17)
+                info, tuned = cbk.autotune("sysvnp_bucketed", "d", 48, 48, nrhs, total)
                 assert info == 0, info
             work = torch.empty(cbk.BUCKETED_LWORK, dtype=torch.uint8, device=dev)
             tup = [(b["n"], b["nm"], V, b["a"], b["n"], b["b"], b["n"]) for b in bks]

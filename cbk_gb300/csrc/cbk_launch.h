@@ -17,9 +17,10 @@ int threads_for(int routine, int n, int dsize);
 void set_threads(int routine, int n, int dsize, int threads);
 
 // Compiled shape of a kernel that has several (0 = the built-in default):
-// 0 / 1 for the warp-per-matrix refined solve's register caps, the refined
-// solve's and least squares' kernel choice; 0 .. 3 for the bucketed launch
-// (the persistent grid's warps per SM halved `variant` times).
+// 0 .. 3 for the warp-per-matrix refined solve (four matrices per block at
+// two register caps, two matrices, one matrix), the least squares' kernel
+// choice; 0 .. 3 for the bucketed launch (the persistent grid's warps per SM
+// halved `variant` times).
 constexpr int MAX_VARIANTS = 4;
 int variant_for(int routine, int n, int dsize);
 void set_variant(int routine, int n, int dsize, int variant);
@@ -124,6 +125,12 @@ cudaError_t launch_posv_refined_warp(bool row, bool up, int n, int nrhs, double 
                                      double *bp, int ldbp, int V, int nm, int max_iter,
                                      int *iters, double *berr, cudaStream_t s, size_t sa_ = 0,
                                      size_t sb_ = 0);
+// the same with two (wpb = 2) or one (wpb = 1) matrices per block
+// (cbk_kernels_refine_warp_small.cu); sa, sb: the group strides
+cudaError_t launch_posv_refined_warp_small(int wpb, bool row, bool up, int n, int nrhs,
+                                           double *ap, int ldap, double *bp, int ldbp, int V,
+                                           int nm, int max_iter, int *iters, double *berr,
+                                           cudaStream_t s, size_t sa, size_t sb);
 
 // the refined solve on host-memory batches, copies pipelined with the solves
 // (cbk_host.cpp); dwork: device workspace of posv_refined_host_lwork bytes

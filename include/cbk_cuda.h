@@ -495,8 +495,10 @@ int cbk_cuda_dposv_refined_compact_noalloc_async(char layout, char uplo, int n, 
 
 /* Autotuning, no reference counterpart. The library keeps one process-wide
  * table of launch shapes per (routine, precision, order): threads per block
- * of the lane-per-matrix kernels, the kernel variant of the warp-per-matrix
- * refined solve (orders 17 .. 64), and the interleave width measured fastest
+ * of the lane-per-matrix kernels, the block shape of the warp-per-matrix
+ * refined solve (orders 17 .. 64: variant 0 four matrices per block, 1 the
+ * same at a lower register cap with one block more per SM, 2 two matrices
+ * per block, 3 one), and the interleave width measured fastest
  * (advice for the caller's packing; a batch's width is the caller's). Entry
  * 0 means the built-in choice. Launch shapes never change results.
  * routine: "potrf", "sytrfnp", "potrs", "posv", "sytrsnp", "sysvnp", "trsm",

@@ -1,6 +1,7 @@
 """The autotuner on the GPU: it measures, keeps a valid winner in the table,
 and no launch shape it can pick changes a result (bit-identical outputs for
-every threads-per-block choice and both refined-kernel variants)."""
+every threads-per-block choice and every block shape of the warp-per-matrix
+refined solve)."""
 import numpy as np
 import pytest
 
@@ -28,7 +29,7 @@ def test_autotune_picks_a_measured_shape(tune, routine, prec, m, n, nrhs, cuda):
     assert r["vlen"] in (32, 64, 128) and r["ms"] > 0
     warp = routine == "posv_refined" and 16 < n <= 64
     if warp:
-        assert r["variant"] in (0, 1) and r["threads"] == 0
+        assert r["variant"] in (0, 1, 2, 3) and r["threads"] == 0
     elif routine == "posv_refined":
         assert r["threads"] in (32, 64, 128)
     else:
@@ -51,7 +52,7 @@ def _solve(tune, A, B, V, refined):
     return ap.cpu().numpy(), bp.cpu().numpy()
 
 
-@pytest.mark.parametrize("n", [8, 24, 48])
+@pytest.mark.parametrize("n", [8, 24, 48, 61])
 def test_launch_shape_never_changes_results(tune, n, cuda):
     rng = np.random.default_rng(n)
     A, _ = C.gen_spd_cond(rng, 3000, n)
@@ -63,7 +64,7 @@ def test_launch_shape_never_changes_results(tune, n, cuda):
     for o in outs[1:]:
         assert all(np.array_equal(x, y) for x, y in zip(outs[0], o))
     outs = []
-    for shape in ((64, 0), (256, 0), (0, 0), (0, 1)):
+    for shape in ((64, 0), (256, 0), (0, 0), (0, 1), (0, 2), (0, 3)):
         assert tune.tune_set("posv_refined", "d", n, threads=shape[0], variant=shape[1]) == 0
         outs.append(_solve(tune, A, B, 32, refined=True))
     for o in outs[1:]:
@@ -98,3 +99,33 @@ def test_bucketed_grid_is_tuned_and_never_changes_results(tune, routine, cuda):
     for o in outs[1:]:
         assert all(np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
                    for x, y in zip(outs[0], o))
+
+
+def test_warp_block_shape_is_searched_and_applied(tune, cuda):
+    """The warp-per-matrix refined solve's block shape (variant 0: four
+    matrices per block, 1: the same at a lower register cap, 2: two matrices,
+    3: one) is a tuning dimension: the autotuner times all four at the order
+    and stores one; a shape set in the table is the one the next launch uses
+    -- its kernel runs (the grid follows the shape) and the solution is the
+    bits of every other shape, with every matrix converged."""
+    import torch
+    info, r = tune.autotune_at("posv_refined", "d", 32, 32, 1, 16384, 32)
+    assert info == 0 and r["variant"] in (0, 1, 2, 3) and r["vlen"] == 32
+    assert tune.tune_get("posv_refined", "d", 32)[1]["variant"] == r["variant"]
+    rng = np.random.default_rng(32)
+    A, _ = C.gen_spd_cond(rng, 777, 32)
+    B = rng.standard_normal((777, 32, 1))
+    ref = None
+    for v in (3, 2, 1, 0):
+        assert tune.tune_set("posv_refined", "d", 32, variant=v) == 0
+        assert tune.tune_get("posv_refined", "d", 32)[1]["variant"] == v
+        ap = torch.from_numpy(O.pack(A, 32)).cuda()
+        bp = torch.from_numpy(O.pack(B, 32, pad_diag=0.0)).cuda()
+        it = torch.empty(777, dtype=torch.int32, device="cuda")
+        assert tune.dposv_refined_compact("C", "L", 32, 1, ap, 32, bp, 32, 32, 777, iters=it) == 0
+        torch.cuda.synchronize()
+        assert int(it.min()) >= 0
+        got = bp.cpu().numpy()
+        if ref is None:
+            ref = got
+        assert np.array_equal(got, ref), v
