@@ -5,7 +5,9 @@
 // caller). cbk_cuda_autotune times a routine on a synthetic batch of nm
 // matrices generated on the device -- uniform entries in [-1, 1), with the
 // diagonal raised by n + 1 where the routine needs a positive-definite or
-// well-conditioned triangular matrix, and the factors computed first where
+// well-conditioned triangular matrix (for the mixed-precision solve, SPD
+// matrices of condition 1e1 .. 1e6: its time depends on the refinement
+// steps), and the factors computed first where
 // the routine consumes them (potrs, sytrsnp: the factor; ormqr, orgqr: the
 // QR) -- for every candidate shape: threads per block 64 / 128 / 256 for the
 // lane-per-matrix kernels (32 / 64 / 128 for the lane-per-matrix refined
@@ -54,6 +56,48 @@ template <typename T> __global__ void k_shift_diag(T *a, int n, int V, long lane
     T *p = a + g * (long)n * n * V + v;
     for (int i = 0; i < n; ++i)
         p[((long)i * n + i) * V] += shift;
+}
+
+// An SPD batch shaped like the mixed-precision solve's work: per lane
+// A = H D H with H = I - 2 v v^T / v^T v (v uniform in [-1, 1)^n: a dense
+// orthogonal H) and D = diag(kappa^-u_i), u_0 = 0 < u_i < u_{n-1} = 1,
+// kappa = 10^(1..6) log-uniform per lane -- condition numbers that a diagonal
+// scaling does not remove, so the refinement takes its usual 2 to 3 steps
+// (a diagonally dominant batch converges in one and times the wrong kernel
+// mix). Written column-major compact, ld = n.
+template <typename T> __global__ void k_fill_spd_reflector(T *a, int n, int V, long lanes,
+                                                           unsigned long long seed)
+{
+    const long l = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (l >= lanes) return;
+    const long g = l / V;
+    const int v0 = (int)(l - g * V);
+    T *p = a + g * (long)n * n * V + v0;
+    auto unif = [&](unsigned long long k) {
+        return (double)(mix64(seed ^ ((unsigned long long)l << 20) ^ k) >> 11) * 0x1p-53;
+    };
+    const double lk = 1.0 + 5.0 * unif(0xFFFFF);
+    double s = 0.0, w = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double vi = 2.0 * unif(2 * i) - 1.0;
+        const double ui = n == 1 ? 0.0 : (i == 0 ? 0.0 : (i == n - 1 ? 1.0 : unif(2 * i + 1)));
+        const double di = exp10(-lk * ui);
+        s += vi * vi;
+        w += di * vi * vi;
+    }
+    for (int j = 0; j < n; ++j) {
+        const double vj = 2.0 * unif(2 * j) - 1.0;
+        const double uj = n == 1 ? 0.0 : (j == 0 ? 0.0 : (j == n - 1 ? 1.0 : unif(2 * j + 1)));
+        const double dj = exp10(-lk * uj);
+        for (int i = 0; i < n; ++i) {
+            const double vi = 2.0 * unif(2 * i) - 1.0;
+            const double ui = n == 1 ? 0.0 : (i == 0 ? 0.0 : (i == n - 1 ? 1.0 : unif(2 * i + 1)));
+            const double di = exp10(-lk * ui);
+            const double aij = (i == j ? di : 0.0) - 2.0 * (di + dj) * vi * vj / s +
+                               4.0 * vi * vj * w / (s * s);
+            p[((long)j * n + i) * V] = (T)aij;
+        }
+    }
 }
 
 template <typename T> struct Batch {
@@ -138,7 +182,10 @@ cudaError_t make_batch(const Spec &sp, int m, int n, int nrhs, int V, int nm, Ba
     const unsigned grid = 1024;
     k_fill_uniform<T><<<grid, 256, 0, s>>>(B.a0, (long)B.sa, 0x5EEDull);
     k_fill_uniform<T><<<grid, 256, 0, s>>>(B.b0, (long)B.sb, 0xB0Bull);
-    if (sp.spd)
+    if (sp.kind == REFINED)
+        k_fill_spd_reflector<T><<<(unsigned)((B.lanes + 127) / 128), 128, 0, s>>>(
+            B.a0, n, V, B.lanes, 0x5EEDull);
+    else if (sp.spd)
         k_shift_diag<T><<<(unsigned)((B.lanes + 255) / 256), 256, 0, s>>>(B.a0, n, V, B.lanes,
                                                                           T(n + 1));
     if ((e = cudaGetLastError())) return e;

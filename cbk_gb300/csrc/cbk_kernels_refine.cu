@@ -48,6 +48,9 @@ namespace {
 
 constexpr double EPS64 = 2.220446049250313e-16;
 constexpr int REG_NMAX = 16;
+// orders whose first residual is taken in double-FP32 arithmetic (above it
+// the register kernel has no registers to spare for it: measured slower)
+constexpr int FF_NMAX = 8;
 
 // packed lower-triangle index (column-major), i >= j
 __host__ __device__ constexpr int tix(int i, int j, int N)
@@ -121,8 +124,54 @@ __device__ __forceinline__ void solve32(const float (&L)[N * (N + 1) / 2], const
     }
 }
 
+// The first step's residual r = b - A x0 in double-FP32 arithmetic on the
+// FP32 pipe (dot2_sub): x0, the FP32 solve, is exact in FP32, and A's entries
+// are split into two FP32 parts (47 bits). Its error stays below
+// 2^-38 ||A|| ||x0|| at these orders, far under the first residual itself
+// (~eps32 ||A|| ||x0||), so the correction it gives is as good as an FP64
+// residual's; the stopping test is only ever taken on an FP64 residual.
+// z: x0 in, the residual rounded to nearest FP32 out; returns
+// its largest magnitude (NaN if any entry is NaN).
 template <int N>
-__global__ void __launch_bounds__(128)
+__device__ __forceinline__ float ff_residual(LV<double> A, LV<double> B, int col, float (&z)[N])
+{
+    float rr[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        rr[k] = 0.f;
+    float rnorm = 0.f;
+    // rows one after another (unrolled rows take more registers and, above
+    // order 8, overflow the instruction cache); each row's result enters at
+    // the end of rr
+#pragma unroll 1
+    for (int i = 0; i < N; ++i) {
+        float s, c;
+        split2_rz_any(B(i, col), s, c);
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            float ah, al;
+            split2_rz(j <= i ? A(i, j) : A(j, i), ah, al);
+            dot2_sub(s, c, ah, al, z[j]);
+        }
+        const float r = s + c;
+        rnorm = fmax_nan(rnorm, fabsf(r));
+#pragma unroll
+        for (int k = 0; k + 1 < N; ++k)
+            rr[k] = rr[k + 1];
+        rr[N - 1] = r;
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        z[k] = rr[k];
+    return rnorm;
+}
+
+// Up to order 8 the registers are capped at 128 (four blocks of 128 threads
+// per SM): measured at n = 8, 16 warps per SM with a few spills beat 12
+// without (0.179 against 0.196 ms for 262,144 matrices); at n = 16 every cap
+// was slower.
+template <int N>
+__global__ void __launch_bounds__(128, N <= FF_NMAX ? 4 : 1)
     k_posv_refined_reg(bool row, bool up, int nrhs, double *ap, int ldap, double *bp, int ldbp,
                        int V, long ngroups, size_t sa, size_t sb, RefineOut out)
 {
@@ -200,27 +249,42 @@ __global__ void __launch_bounds__(128)
             x[i] = f2d_int(z[i]);
         float rprev = INFINITY;
         for (int it = 0;; ++it) {
-            // opaque strides: the n^2 addresses of A are recomputed each step
-            // (cheap integer work) instead of being hoisted into registers
-            LV<double> Ar = A;
-            asm volatile("" : "+l"(Ar.si), "+l"(Ar.sj));
             float rnorm = 0.f, xnorm = 0.f;
+            bool fp64 = true;
+            if (N <= FF_NMAX && it == 0) {
+                // x0 is z: the double-FP32 residual, unless x0 may already
+                // meet the test (then the FP64 residual below decides)
 #pragma unroll
-            for (int i = 0; i < N; ++i) {
-                double acc = B(i, col);
-#pragma unroll
-                for (int j = 0; j < N; ++j)
-                    acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
-                z[i] = d2f_rz(acc);
-                rnorm = fmax_nan(rnorm, fabsf(z[i]));
-                xnorm = fmaxf(xnorm, fabsf(d2f_rz_inrange(x[i])));
+                for (int i = 0; i < N; ++i)
+                    xnorm = fmaxf(xnorm, fabsf(z[i]));
+                rnorm = ff_residual<N>(A, B, col, z);
+                fp64 = !(rnorm > cte32 * xnorm + 0x1p-38f * anorm * xnorm);
             }
-            const float thr = cte32 * xnorm;
-            if (thr >= 0x1p-100f ? rnorm <= thr : (double)rnorm <= cte * (double)xnorm) {
-                const float den = anorm * xnorm + bnorm;
-                worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
-                it_max = max(it_max, it);
-                break;
+            if (fp64) {
+                // opaque strides: the n^2 addresses of A are recomputed each
+                // step (cheap integer work) instead of being hoisted into
+                // registers
+                LV<double> Ar = A;
+                asm volatile("" : "+l"(Ar.si), "+l"(Ar.sj));
+                rnorm = 0.f;
+                xnorm = 0.f;
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    double acc = B(i, col);
+#pragma unroll
+                    for (int j = 0; j < N; ++j)
+                        acc = fma(-(j <= i ? Ar(i, j) : Ar(j, i)), x[j], acc);
+                    z[i] = d2f_rz(acc);
+                    rnorm = fmax_nan(rnorm, fabsf(z[i]));
+                    xnorm = fmaxf(xnorm, fabsf(d2f_rz_inrange(x[i])));
+                }
+                const float thr = cte32 * xnorm;
+                if (thr >= 0x1p-100f ? rnorm <= thr : (double)rnorm <= cte * (double)xnorm) {
+                    const float den = anorm * xnorm + bnorm;
+                    worst = fmaxf(worst, den > 0.f ? rnorm / den : 0.f);
+                    it_max = max(it_max, it);
+                    break;
+                }
             }
             if (it >= out.max_iter || !(rnorm <= 0.5f * rprev)) {
                 status = -3;
@@ -417,7 +481,10 @@ cudaError_t launch_posv_refined(bool row, bool up, int n, int nrhs, double *ap, 
     const size_t sb = sb_ ? sb_ : gstride(row, ldbp, n, nrhs, V);
     const RefineOut out{iters, berr, nm, max_iter};
     // the lane-per-matrix variants are compiled for at most 128 threads
-    const int th = std::min(threads_for(R_POSV_REFINED, n, sizeof(double)), 128);
+    // built-in: 64 threads per block up to order 8 (measured fastest there
+    // with the register cap), 128 above
+    const int th =
+        std::min(threads_or(R_POSV_REFINED, n, sizeof(double), n <= FF_NMAX ? 64 : 128), 128);
     const unsigned bl = (unsigned)((ng * V + th - 1) / th);
     if (n <= REG_NMAX) {
         switch (n) {

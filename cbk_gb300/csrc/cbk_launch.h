@@ -14,6 +14,8 @@ namespace cbkcuda {
 // Threads per block of the lane-per-matrix kernels (the autotuner may change
 // it per routine and order; 0 selects the built-in default).
 int threads_for(int routine, int n, int dsize);
+// the same with the built-in choice dflt
+int threads_or(int routine, int n, int dsize, int dflt);
 void set_threads(int routine, int n, int dsize, int threads);
 
 // Compiled shape of a kernel that has several (0 = the built-in default):

@@ -77,7 +77,7 @@ int slot_of(int n)
 
 } // namespace
 
-int threads_for(int routine, int n, int dsize)
+int threads_or(int routine, int n, int dsize, int dflt)
 {
     if (int f = forced()) return f;
     load_env_file();
@@ -85,7 +85,12 @@ int threads_for(int routine, int n, int dsize)
     const int t = (routine >= 0 && routine < R_COUNT)
                       ? g_table[routine][dsize == 8 ? 1 : 0][slot].load(std::memory_order_relaxed)
                       : 0;
-    return t > 0 ? t : 128;
+    return t > 0 ? t : dflt;
+}
+
+int threads_for(int routine, int n, int dsize)
+{
+    return threads_or(routine, n, dsize, 128);
 }
 
 void set_threads(int routine, int n, int dsize, int threads)
