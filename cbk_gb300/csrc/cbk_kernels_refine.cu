@@ -258,7 +258,9 @@ __global__ void __launch_bounds__(128, N <= FF_NMAX ? 4 : 1)
                 for (int i = 0; i < N; ++i)
                     xnorm = fmaxf(xnorm, fabsf(z[i]));
                 rnorm = ff_residual<N>(A, B, col, z);
-                fp64 = !(rnorm > cte32 * xnorm + 0x1p-38f * anorm * xnorm);
+                // FP64 unless clearly unconverged and finite (an FP32
+                // overflow in the products is no reason to fall back)
+                fp64 = !(rnorm > cte32 * xnorm + 0x1p-38f * anorm * xnorm && rnorm <= FLT_MAX);
             }
             if (fp64) {
                 // opaque strides: the n^2 addresses of A are recomputed each
