@@ -39,7 +39,9 @@ line under "configs" (each with its own roofline and a cpu_baseline through
 the reference's own build on the same matrices): c1 plain dposv n = 8 on
 65,536 matrices; c2 dgels 16 x 8 (nrhs 4) and dorgqr on 1,048,576; c4 the
 uneven-order dsysvnp in one CUDA-graph launch against one launch per order;
-c5 the mixed-precision least squares 64 x 16 (nrhs 8) against plain dgels.
+c5 the mixed-precision least squares 64 x 16 (nrhs 8) against plain dgels;
+lay the layout / triangle / side / transpose forms of posv (plain and
+refined), trsm and ormqr, each against its column-major lower / left form.
 --config NAME prints one of them (or c3d: the headline's refined solve on
 strided dense batches against the compact layout) on its own line; --no-extra
 leaves them out. --case KIND N NM runs one small solve for a profiler
@@ -729,7 +731,7 @@ def run_gpu(args):
     torch.cuda.empty_cache()
     if ws == 1 and not args.no_extra:
         t0 = time.perf_counter()
-        line["configs"] = config_lines(("c1", "c2", "c4", "c5"), args, cbk, dev,
+        line["configs"] = config_lines(("c1", "c2", "c4", "c5", "lay"), args, cbk, dev,
                                        with_cpu=not args.no_cpu)
         line["configs_wall_s"] = time.perf_counter() - t0
     if rank == 0:
@@ -1157,6 +1159,85 @@ def config_lines(names, args, cbk, dev, with_cpu=True):
                     "gels", (Ad.cpu().numpy(), Bd.cpu().numpy()), UNIT)
                 line["cpu_baseline"]["sample"] += " (the reference's plain FP64 dgels_compact)"
             del ap0, bp0, Ad, Bd, ap, bp, tau, work
+        elif name == "lay":
+            # The layout, triangle, side and transpose variants that the
+            # configurations above run in one form only: each routine timed in
+            # every form on the same bytes (a symmetric matrix reads the same in
+            # either layout and triangle; a random square one is a valid
+            # triangular or QR input in any of them), against its column-major
+            # lower / left form.
+            variants = {}
+
+            def ratio_table(key, times):
+                base = times[next(iter(times))]
+                variants[key] = {"ms": times, "worst_over_first": max(times.values()) / base}
+            for n in (16, 48):
+                nm = 65536
+                G = torch.randn(nm, n, n, dtype=f64, device=dev, generator=gen)
+                A = G @ G.transpose(1, 2) + n * torch.eye(n, dtype=f64, device=dev)
+                B = torch.randn(nm, n, 1, dtype=f64, device=dev, generator=gen)
+                ap0, bp0 = pack_dev(cbk, A), pack_dev(cbk, B)
+                ap, bp = ap0.clone(), bp0.clone()
+                work = torch.empty(max(1, cbk.dposv_refined_lwork(n, 1, V, nm)),
+                                   dtype=torch.uint8, device=dev)
+
+                def restore():
+                    ap.copy_(ap0)
+                    bp.copy_(bp0)
+                for kind in ("posv", "posv_refined"):
+                    times = {}
+                    for lay, uplo in (("C", "L"), ("C", "U"), ("R", "L"), ("R", "U")):
+                        if kind == "posv":
+                            fn = (lambda lay=lay, uplo=uplo: cbk.check("posv", cbk.dposv_compact(
+                                lay, uplo, n, 1, ap, n, bp, 1 if lay == "R" else n, V, nm)) or 1)
+                        else:
+                            fn = (lambda lay=lay, uplo=uplo: cbk.check(
+                                "posv_refined", cbk.dposv_refined_compact(
+                                    lay, uplo, n, 1, ap, n, bp, 1 if lay == "R" else n, V, nm, 10,
+                                    None, None, work)) or 1)
+                        times[f"{lay},{uplo}"], _ = timed(fn, restore, args.steps, args.warmup)
+                    ratio_table(f"d{kind} n={n} (layout,uplo)", times)
+                del G, A, B, ap0, bp0, ap, bp, work
+            m, nm = 16, 1 << 18
+            T0 = torch.randn(nm, m, m, dtype=f64, device=dev, generator=gen)
+            T0 = T0 + 4.0 * m * torch.eye(m, dtype=f64, device=dev)
+            C0 = torch.randn(nm, m, m, dtype=f64, device=dev, generator=gen)
+            tp0, cp0 = pack_dev(cbk, T0), pack_dev(cbk, C0)
+            tp, cp = tp0.clone(), cp0.clone()
+
+            def restore_c():
+                cp.copy_(cp0)
+            times = {}
+            for lay in ("C", "R"):
+                for side in ("L", "R"):
+                    for tr in ("N", "T"):
+                        times[f"{lay},{side},{tr}"], _ = timed(
+                            lambda lay=lay, side=side, tr=tr: cbk.check("trsm", cbk.dtrsm_compact(
+                                lay, side, "L", tr, "N", m, m, 1.0, tp, m, cp, m, V, nm)) or 1,
+                            restore_c, args.steps, args.warmup)
+            ratio_table("dtrsm 16x16, 16 right-hand sides (layout,side,trans)", times)
+            times = {}
+            k = 8
+            tau = torch.empty(nm * k, dtype=f64, device=dev)
+            for lay in ("C", "R"):
+                tp.copy_(tp0)
+                lda = m if lay == "C" else k  # the QR of the leading 16 x 8 block
+                cbk.check("geqrf", cbk.dgeqrf_compact(lay, m, k, tp, lda, tau, V, nm))
+                for side, tr in (("L", "T"), ("R", "N")):
+                    times[f"{lay},{side},{tr}"], _ = timed(
+                        lambda lay=lay, side=side, tr=tr, lda=lda: cbk.check(
+                            "ormqr", cbk.dormqr_compact(lay, side, tr, m, m, k, tp, lda, tau, cp,
+                                                        m, V, nm)) or 1,
+                        restore_c, args.steps, args.warmup)
+            ratio_table("dormqr 16x16, k=8 (layout,side,trans)", times)
+            del T0, C0, tp0, cp0, tp, cp, tau
+            line.update(metric="layout / triangle / side variants against the first form (ms)",
+                        value=max(v["worst_over_first"] for v in variants.values()),
+                        unit="worst time ratio", higher_is_better=False, dtype="f64",
+                        data="synthetic: SPD G G^T + n I; triangular T + 4m I; C ~ N(0,1)",
+                        variants=variants, gpu_launches=args.steps)
+            line["config"]["workload"] = ("dposv (plain, refined) n=16/48 x 65536, dtrsm and "
+                                          "dormqr 16x16 x 262144, V=32, every form")
         torch.cuda.empty_cache()
         out[name] = line
     return out
@@ -1185,7 +1266,8 @@ def main():
                     help="skip the other configurations (c1, c2, c4, c5) in the headline line")
     ap.add_argument("--ref-per-n", type=int, default=NM,
                     help="--impl reference: matrices per order (default: the whole workload)")
-    ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5", "c3d"), default="c3",
+    ap.add_argument("--config", choices=("c3", "c1", "c2", "c4", "c5", "c3d", "lay"),
+                    default="c3",
                     help="c3 (default) is the headline; the others print their own line")
     ap.add_argument("--case", nargs=3, metavar=("KIND", "N", "NM"),
                     help="no timing: solve one batch (refined|plain, order N, NM matrices) "
