@@ -5,7 +5,7 @@ benchmark orders, the mixed-precision solves on all their kernels, the
 bucketed launch and pack / unpack (tests/checked_run.py, in a process of its
 own); no access may be refused, and every result must still be the oracle's.
 This is the out-of-bounds read and write detection that replaces a
-sanitizer, which is not available on this GPU pool."""
+sanitizer, which these tests cannot run."""
 import os
 import re
 import subprocess

@@ -8,8 +8,8 @@ lanes and untouched triangles -- must agree to the last bit, over every
 routine, both precisions, the reference's widths 2/4/8/16 and (by
 re-interleaving at 16 lanes) the GPU widths 32/64.
 
-Skipped where the reference's sources are absent (the GPU machine): the golden
-fixtures carry the pin there (test_oracle_golden.py).
+Skipped where the reference's sources are absent: the golden fixtures carry
+the pin there (test_oracle_golden.py).
 """
 import numpy as np
 import pytest
