@@ -237,36 +237,49 @@ __device__ __forceinline__ double f2d_int(float f, int shift = 0)
     return __hiloint2double((int)hi, (int)(mant << 29));
 }
 
-// a = hi + lo + d on the integer pipe: hi = a toward zero to 24 significant
-// bits, lo = the next 23 bits toward zero (exact: a 23-bit integer times a
-// power of two), |d| < 2^-47 |a|. For |a| < 2^128 (callers screen the range);
-// hi = lo = 0 below the FP32 normal range.
-__device__ __forceinline__ void split2_rz(double a, float &hi, float &lo)
+// a 2^sh = hi + lo + d on the integer pipe: hi = a 2^sh toward zero to 24
+// significant bits, lo = the next 23 bits toward zero (exact: a 23-bit integer
+// times a power of two), |d| < 2^-47 |a 2^sh|; the power of two only moves the
+// exponent. For |a 2^sh| < 2^128 (callers screen the range); hi = lo = 0 below
+// the FP32 normal range.
+__device__ __forceinline__ void split2_rz(double a, float &hi, float &lo, int sh = 0)
 {
     const unsigned h = (unsigned)__double2hiint(a), l = (unsigned)__double2loint(a);
     const unsigned sign = h & 0x80000000u;
     const int e = (int)((h >> 20) & 0x7ffu);
-    const int fe = e - 896;
+    const int fe = e - 896 + sh;
     const unsigned hb = sign | ((unsigned)fe << 23) | ((h & 0xfffffu) << 3) | (l >> 29);
     hi = __uint_as_float(fe > 0 ? hb : sign);
     // bits 28..6 of l as an integer: exact in FP32 through the 2^23 offset
     const float m = __uint_as_float(0x4b000000u | ((l >> 6) & 0x7fffffu)) - 8388608.0f;
-    // their weight 2^(e - 1069): FP32 exponent field e - 942 (zero below range)
-    const int se = e - 942;
+    // their weight 2^(e - 1069 + sh): FP32 exponent field e - 942 + sh (zero
+    // below range)
+    const int se = e - 942 + sh;
     lo = m * __uint_as_float(sign | ((unsigned)(se > 0 ? se : 0) << 23));
 }
 
 // The same for any a: beyond the FP32 range hi is an infinity (a NaN stays a
 // NaN) and lo is 0.
-__device__ __forceinline__ void split2_rz_any(double a, float &hi, float &lo)
+__device__ __forceinline__ void split2_rz_any(double a, float &hi, float &lo, int sh = 0)
 {
     const int e = (int)(((unsigned)__double2hiint(a) >> 20) & 0x7ffu);
-    if (e >= 1151) {
-        hi = d2f_rz(a);
+    if (e + sh >= 1151) {
+        hi = d2f_rz(a, sh);
         lo = 0.f;
         return;
     }
-    split2_rz(a, hi, lo);
+    split2_rz(a, hi, lo, sh);
+}
+
+// (s, c) := (s, c) + (s2, c2), both double-FP32 values (TwoSum on the leading
+// parts, the rest into c)
+__device__ __forceinline__ void dd_add(float &s, float &c, float s2, float c2)
+{
+    const float t = s + s2;
+    const float bb = t - s;
+    const float err = (s - (t - bb)) + (s2 - bb);
+    s = t;
+    c = (c + c2) + err;
 }
 
 // (s, c) := (s, c) - a x in double-FP32 arithmetic, a = ah + al, x exact:

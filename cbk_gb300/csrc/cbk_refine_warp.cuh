@@ -313,6 +313,64 @@ __device__ __forceinline__ void residual(int lane, const double *SA, const doubl
     }
 }
 
+// (s, c) of this lane's rows := (s, c) - (D A D) v in double-FP32 arithmetic
+// (dot2_sub), with v = SV[0 .. N) broadcast from shared memory and the scaled
+// entries d_i a_ij d_j of the packed FP64 triangle split on the integer pipe
+// (D = diag(2^-SH[i]): the scaling is an exponent shift). The rows are
+// residual<N>'s: row lane over all columns and, for N <= 48, row 32 + lane % 16
+// by column halves, the lower half carrying the row's running value and the
+// two halves' sums joined with one exchange (both then hold the row's total);
+// for N > 48 row lane + 32 over all columns.
+template <int N>
+__device__ __forceinline__ void ff_update(int lane, const double *SA, const int *SH,
+                                          const float *SV, float (&s)[(N + 31) / 32],
+                                          float (&c)[(N + 31) / 32])
+{
+    constexpr int NR = (N + 31) / 32;
+    constexpr int H = N / 2;
+    const int i0 = min(lane, N - 1); // lanes past N (N < 32) compute a row they discard
+    const int c0 = pk_col(N, i0) - i0;
+    const int h0 = SH[i0];
+    // columns in groups of 8 (a fully unrolled row is code the instruction
+    // cache cannot hold beside the sweep's)
+#pragma unroll 8
+    for (int t = 0; t < N; ++t) {
+        float ah, al;
+        split2_rz(SA[t <= i0 ? i0 + (pk_col(N, t) - t) : c0 + t], ah, al, -(h0 + SH[t]));
+        dot2_sub(s[0], c[0], ah, al, SV[t]);
+    }
+    if constexpr (NR == 2) {
+        if constexpr (N <= 48) {
+            const bool lower = lane < 16;
+            const int i1 = min(32 + (lane & 15), N - 1);
+            const int c1 = pk_col(N, i1) - i1;
+            const int h1 = SH[i1];
+            float s1 = lower ? s[1] : 0.f, k1 = lower ? c[1] : 0.f;
+#pragma unroll 8
+            for (int t = 0; t < H; ++t) {
+                const int j = (lower ? 0 : H) + t;
+                float ah, al;
+                split2_rz(SA[j <= i1 ? i1 + (pk_col(N, j) - j) : c1 + j], ah, al, -(h1 + SH[j]));
+                dot2_sub(s1, k1, ah, al, SV[j]);
+            }
+            dd_add(s1, k1, __shfl_xor_sync(FULL, s1, 16), __shfl_xor_sync(FULL, k1, 16));
+            s[1] = s1;
+            c[1] = k1;
+        }
+        else {
+            const int i1 = min(lane + 32, N - 1);
+            const int c1 = pk_col(N, i1) - i1;
+            const int h1 = SH[i1];
+#pragma unroll 8
+            for (int t = 0; t < N; ++t) {
+                float ah, al;
+                split2_rz(SA[t <= i1 ? i1 + (pk_col(N, t) - t) : c1 + t], ah, al, -(h1 + SH[t]));
+                dot2_sub(s[1], c[1], ah, al, SV[t]);
+            }
+        }
+    }
+}
+
 template <int N, int WPB, int MINB>
 __global__ void __launch_bounds__(WPB * 32, MINB)
     k_posv_refined_warp(bool row, bool up, int n, int nrhs, double *ap, int ldap, double *bp,
@@ -628,6 +686,22 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
         }
     }
     if (nonpos && status == 0) status = -1;
+    // up to order 40 the first residual is taken in double-FP32 (below); it
+    // needs the row scales h of every row, kept in the sweep's column buffers
+    // (free now)
+    constexpr bool FF_FIRST = N <= 40;
+    int *const SH = reinterpret_cast<int *>(SC);
+    if constexpr (FF_FIRST) {
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+            if (lane + 32 * r < N) SH[lane + 32 * r] = h[r];
+    }
+    // this lane's residual rows: lane, and lane + 32 or (N <= 48) 32 + lane % 16
+    const int i0 = min(lane, N - 1);
+    const int i1 = min(L::SPLIT ? 32 + (lane & 15) : lane + 32, N - 1);
+    const bool real0 = lane < n;
+    const bool real1 = NR == 2 && (L::SPLIT ? lane < 16 : true) && lane + 32 < n;
 
     // LAPACK dsposv's test ||r|| <= sqrt(n) eps64 ||A|| ||x||, in FP32 while
     // the right side is a normal FP32 number, in FP64 below that
@@ -660,32 +734,75 @@ __global__ void __launch_bounds__(WPB * 32, MINB)
             if (i < N) SX[i] = x;
         }
         xn = warp_max(xn);
+        // Up to order 40 the first residual is taken in double-FP32 on the
+        // FP32 pipe: rs + rc = D b - (D A D) w0, w0 = D^-1 x0 exact in FP32
+        // (Dot2 over the two-float split of A, ff_update). Its error, near
+        // n 2^-48 ||A|| ||x||, is far below the first residual (about eps32
+        // ||A|| ||x||), so the first correction is as good as from an FP64
+        // residual; every later residual, and every stopping test, is FP64
+        // (a correction from a double-FP32 residual would leave its error in
+        // x). Measured at 262,144 matrices: n = 24 1.40 against 1.65 ms,
+        // n = 32 1.78 against 2.01, n = 40 4.17 against 4.31; from n = 48 on
+        // the extra code in a kernel at its register cap cost more than the
+        // FP64 residual it saves (5.64 against 5.41 ms), so it is left out.
         float rprev = INFINITY;
         for (int it = 0;; ++it) {
-            __syncwarp();
-            double acc[NR];
-#pragma unroll
-            for (int r = 0; r < NR; ++r)
-                acc[r] = (lane + 32 * r < N) ? SB[lane + 32 * r] : 0.0;
-            residual<N>(lane, SA, SX, acc, acc);
+            bool fp64 = true;
             float rn = 0.f;
-            bool nan = false; // fmaxf drops a NaN: a NaN residual must stop the refinement
+            if (FF_FIRST && it == 0) {
+                float rs_[NR], rc_[NR];
+                __syncwarp();
 #pragma unroll
-            for (int r = 0; r < NR; ++r) {
-                const bool real = lane + 32 * r < n;
-                const float v = real ? fabsf(d2f_rz(acc[r])) : 0.f;
-                nan |= v != v;
-                rn = fmaxf(rn, v);
-                w[r] = real ? d2f_rz(acc[r], -h[r]) : 0.f;
+                for (int r = 0; r < NR; ++r)
+                    if (lane + 32 * r < N) SR[lane + 32 * r] = (lane + 32 * r < n) ? w[r] : 0.f;
+                __syncwarp();
+                split2_rz_any(SB[i0], rs_[0], rc_[0], -SH[i0]);
+                if constexpr (NR == 2) split2_rz_any(SB[i1], rs_[1], rc_[1], -SH[i1]);
+                ff_update<N>(lane, SA, SH, SR, rs_, rc_);
+                bool nan = false;
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    const bool real = r == 0 ? real0 : real1;
+                    const float v = real ? fabsf(rs_[r] + rc_[r]) * exp2i(SH[r == 0 ? i0 : i1]) : 0.f;
+                    nan |= v != v;
+                    rn = fmaxf(rn, v);
+                }
+                rn = warp_max(rn);
+                // FP64 unless clearly above the stopping threshold and finite
+                const float clear = cte32 * xn + 0x1p-40f * anorm * xn;
+                fp64 = __any_sync(FULL, nan) || !(rn > clear && rn <= FLT_MAX);
+                if (!fp64) {
+#pragma unroll
+                    for (int r = 0; r < NR; ++r)
+                        w[r] = (lane + 32 * r < n) ? rs_[r] + rc_[r] : 0.f;
+                }
             }
-            rn = __any_sync(FULL, nan) ? NAN : warp_max(rn);
-            const float thr = cte32 * xn;
-            const bool done = thr >= 0x1p-100f ? rn <= thr : (double)rn <= cte * (double)xn;
-            if (done) {
-                const float den = anorm * xn + bn;
-                worst = fmaxf(worst, den > 0.f ? rn / den : 0.f);
-                it_max = max(it_max, it);
-                break;
+            if (fp64) {
+                __syncwarp();
+                double acc[NR];
+#pragma unroll
+                for (int r = 0; r < NR; ++r)
+                    acc[r] = (lane + 32 * r < N) ? SB[lane + 32 * r] : 0.0;
+                residual<N>(lane, SA, SX, acc, acc);
+                rn = 0.f;
+                bool nan = false; // fmaxf drops a NaN: a NaN residual must stop the refinement
+#pragma unroll
+                for (int r = 0; r < NR; ++r) {
+                    const bool real = lane + 32 * r < n;
+                    const float v = real ? fabsf(d2f_rz(acc[r])) : 0.f;
+                    nan |= v != v;
+                    rn = fmaxf(rn, v);
+                    w[r] = real ? d2f_rz(acc[r], -h[r]) : 0.f;
+                }
+                rn = __any_sync(FULL, nan) ? NAN : warp_max(rn);
+                const float thr = cte32 * xn;
+                const bool done = thr >= 0x1p-100f ? rn <= thr : (double)rn <= cte * (double)xn;
+                if (done) {
+                    const float den = anorm * xn + bn;
+                    worst = fmaxf(worst, den > 0.f ? rn / den : 0.f);
+                    it_max = max(it_max, it);
+                    break;
+                }
             }
             if (it >= out.max_iter || !(rn <= 0.5f * rprev)) {
                 status = -3;
