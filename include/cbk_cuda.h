@@ -283,7 +283,10 @@ int cbk_cuda_sunpack_compact_async(char layout, int m, int n, const float *ap, i
  * of each right-hand side, FP64 fallback per matrix. No reference entry
  * point: the ?posv_compact arguments (include/cbk.h:196-212) plus the method
  * of LAPACK dsposv. Per lane: x = solve32(b); r = b - A x in FP64 until
- * ||r||_inf <= sqrt(n) eps64 ||A||_inf ||x||_inf, correcting x += solve32(r);
+ * ||r||_inf <= sqrt(n) eps64 ||A||_inf ||x||_inf, correcting x += solve32(r)
+ * (for n <= 8 and 17 <= n <= 40 the first r, of the FP32-exact x0, is formed
+ * in double-FP32 arithmetic instead: error-free products and sums, Dot2; the
+ * stopping test is always taken on an FP64 residual);
  * a lane whose FP32 rounding overflows (iters = -2), whose FP32 pivot is not
  * positive (-1), or whose refinement stalls or exceeds max_iter corrections
  * (-3) is solved by the FP64 path instead and then holds its FP64 factor in
