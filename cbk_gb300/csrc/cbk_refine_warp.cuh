@@ -318,9 +318,10 @@ __device__ __forceinline__ void residual(int lane, const double *SA, const doubl
 // entries d_i a_ij d_j of the packed FP64 triangle split on the integer pipe
 // (D = diag(2^-SH[i]): the scaling is an exponent shift). The rows are
 // residual<N>'s: row lane over all columns and, for N <= 48, row 32 + lane % 16
-// by column halves, the lower half carrying the row's running value and the
+// by column halves, the lower half carrying the row's starting value and the
 // two halves' sums joined with one exchange (both then hold the row's total);
-// for N > 48 row lane + 32 over all columns.
+// for N > 48 row lane + 32 over all columns (the kernel takes this path up to
+// N = 40 only; the routine holds for any N).
 template <int N>
 __device__ __forceinline__ void ff_update(int lane, const double *SA, const int *SH,
                                           const float *SV, float (&s)[(N + 31) / 32],
@@ -331,8 +332,7 @@ __device__ __forceinline__ void ff_update(int lane, const double *SA, const int 
     const int i0 = min(lane, N - 1); // lanes past N (N < 32) compute a row they discard
     const int c0 = pk_col(N, i0) - i0;
     const int h0 = SH[i0];
-    // columns in groups of 8 (a fully unrolled row is code the instruction
-    // cache cannot hold beside the sweep's)
+    // columns in groups of 8, to keep the kernel's code small
 #pragma unroll 8
     for (int t = 0; t < N; ++t) {
         float ah, al;
