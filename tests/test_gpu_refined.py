@@ -86,6 +86,28 @@ def test_refined_meets_fp64_backward_error(n, layout, uplo, cuda):
           f"worst berr {berr.max() / EPS:.2f} eps, fallbacks {np.unique(it[fell])}")
 
 
+@pytest.mark.parametrize("n", [5, 8, 16, 24, 33, 40, 48, 70])
+def test_refined_exact_fp32_solution_takes_no_correction(n, cuda):
+    """A diagonal of powers of two with a right-hand side exact in FP32: the
+    FP32 solve is already exact, so r0 = 0 and every kernel (register, warp
+    with and without the double-FP32 first residual, workspace) must accept
+    x0 with zero corrections -- through the FP64 residual, since a
+    double-FP32 one that is not clearly above the threshold hands the step to
+    FP64 -- and return x = b / d bit for bit."""
+    rng = np.random.default_rng(77 + n)
+    nm, V = 96, 32
+    k = 2 * rng.integers(-20, 21, size=(nm, n))          # even exponents: sqrt exact
+    d = np.ldexp(1.0, k)
+    A = np.zeros((nm, n, n))
+    A[:, np.arange(n), np.arange(n)] = d
+    B = rng.standard_normal((nm, n, 1)).astype(np.float32).astype(np.float64)
+    info, X, a1, a0, it, be = _run(A, B, V)
+    assert info == 0
+    assert (it == 0).all(), np.unique(it)
+    assert np.array_equal(X, B / d[:, :, None])
+    assert (be == 0).all()
+
+
 def test_refined_fallback_codes(cuda):
     """-2: an entry overflows FP32; -1: the FP32 factor breaks down
     (indefinite in FP32, SPD in FP64); -3: max_iter = 0 with an inexact FP32
