@@ -121,6 +121,42 @@ def dposv_refined_batched(uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm,
 __all__ += ["dposv_refined_batched", "dposv_refined_batched_lwork"]
 
 
+def _plain_batched(prefix, routine):
+    """?posv_batched / ?sysvnp_batched (uplo, n, nrhs, a, lda, stride_a, b,
+    ldb, stride_b, nm) and ?gels_batched (trans, m, n, nrhs, a, lda,
+    stride_a, b, ldb, stride_b, tau, nm): the plain drivers on strided dense
+    batches (arrays: CUDA tensors or device pointers)."""
+    import ctypes
+
+    def f(*args, stream=None):
+        from ._abi import _ptr, _stream, lib
+        fn = getattr(lib(), f"cbk_cuda_{prefix}{routine}_batched_async")
+        fn.restype = ctypes.c_int
+        P, I, L = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+        if routine == "gels":
+            trans, m, n, nrhs, a, lda, sa, b, ldb, sb, tau, nm = args
+            fn.argtypes = [ctypes.c_char, I, I, I, P, I, L, P, I, L, P, I, P]
+            arrays = (a, b, tau)
+            return fn(trans.encode(), m, n, nrhs, _ptr(a, prefix), lda, sa, _ptr(b, prefix), ldb,
+                      sb, _ptr(tau, prefix), nm,
+                      _stream(stream) if any(t is not None and not isinstance(t, int)
+                                             for t in arrays) or stream else None)
+        uplo, n, nrhs, a, lda, sa, b, ldb, sb, nm = args
+        fn.argtypes = [ctypes.c_char, I, I, P, I, L, P, I, L, I, P]
+        return fn(uplo.encode(), n, nrhs, _ptr(a, prefix), lda, sa, _ptr(b, prefix), ldb, sb, nm,
+                  _stream(stream) if (a is not None and not isinstance(a, int)) or stream
+                  else None)
+
+    f.__name__ = f"{prefix}{routine}_batched"
+    return f
+
+
+for _r in ("posv", "sysvnp", "gels"):
+    for _p in ("d", "s"):
+        globals()[f"{_p}{_r}_batched"] = _plain_batched(_p, _r)
+        __all__.append(f"{_p}{_r}_batched")
+
+
 def dgels_refined_batched_lwork(m: int, n: int, nrhs: int, nm: int) -> int:
     """Workspace bytes of dgels_refined_batched (-1: illegal argument)."""
     import ctypes

@@ -314,6 +314,55 @@ int posv_refined_batched(char uplo, int n, int nrhs, double *a, int lda, long lo
                                            (size_t)stride_b));
 }
 
+// The plain FP64 / FP32 drivers on a strided dense batch: the compact layout
+// at V = 1 with the caller's group strides, so the lane kernels read and
+// write the dense arrays directly (no pack or unpack pass), matrix by matrix
+// with the compact entry point's operations (identical bits). ?posv_batched /
+// ?sysvnp_batched: -1 uplo -2 n -3 nrhs -5 lda -6 stride_a -8 ldb -9 stride_b
+// -10 nm; nrhs = 0 still factors (as the compact drivers).
+template <typename T>
+int sym_solve_batched(bool ldlt, char uplo, int n, int nrhs, T *a, int lda, long long stride_a,
+                      T *b, int ldb, long long stride_b, int nm, cudaStream_t s)
+{
+    const bool lo = opt(uplo, 'L'), up = opt(uplo, 'U');
+    if (!lo && !up) return -1;
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (lda < max1(n)) return -5;
+    if (stride_a < (long long)lda * n) return -6;
+    if (ldb < max1(n)) return -8;
+    if (stride_b < (long long)ldb * nrhs) return -9;
+    if (nm < 0) return -10;
+    if (n == 0 || nm == 0) return 0;
+    if (nrhs == 0)
+        return cuda_status(launch_factor<T>(ldlt, false, up, n, a, lda, 1, nm, s, (size_t)stride_a));
+    return cuda_status(launch_sym_solve<T>(ldlt, true, false, up, n, nrhs, a, lda, b, ldb, 1, nm, s,
+                                           (size_t)stride_a, (size_t)stride_b));
+}
+
+// ?gels_batched: A m x n at a + k stride_a, B max(m, n) x nrhs at
+// b + k stride_b, the min(m, n) tau values at tau + k min(m, n).
+// -1 trans -2 m -3 n -4 nrhs -6 lda -7 stride_a -9 ldb -10 stride_b -12 nm.
+template <typename T>
+int gels_batched(char trans, int m, int n, int nrhs, T *a, int lda, long long stride_a, T *b,
+                 int ldb, long long stride_b, T *tau, int nm, cudaStream_t s)
+{
+    const int mx = m > n ? m : n;
+    if (!opt(trans, 'N') && !opt(trans, 'T') && !opt(trans, 'C')) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (lda < max1(m)) return -6;
+    if (stride_a < (long long)lda * n) return -7;
+    if (ldb < max1(mx)) return -9;
+    if (stride_b < (long long)ldb * nrhs) return -10;
+    if (nm < 0) return -12;
+    if (nrhs == 0 || nm == 0 || mx == 0) return 0;
+    const bool tran = opt(trans, 'T') || opt(trans, 'C');
+    return cuda_status(launch_gels<T>(false, tran, m, n, nrhs, a, lda, b, ldb, tau, 1, nm, s,
+                                      (size_t)stride_a, (size_t)stride_b));
+}
+
 // The refined least squares on a strided dense batch (A m x n at
 // a + k stride_a, B m x nrhs at b + k stride_b, column-major; tau n per
 // matrix at tau + k n): the compact layout at V = 1 with these strides.
@@ -842,6 +891,32 @@ int cbk_cuda_dposv_refined_batched_async(char uplo, int n, int nrhs, double *a, 
     return posv_refined_batched(uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm, max_iter,
                                 iters, berr, work, lwork, S(st));
 }
+
+#define CBK_PLAIN_BATCHED(P, T)                                                                    \
+    int cbk_cuda_##P##posv_batched_async(char uplo, int n, int nrhs, T *a, int lda,                \
+                                         long long stride_a, T *b, int ldb, long long stride_b,    \
+                                         int nm, cbk_stream_t st)                                  \
+    {                                                                                              \
+        return sym_solve_batched<T>(false, uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm,  \
+                                    S(st));                                                        \
+    }                                                                                              \
+    int cbk_cuda_##P##sysvnp_batched_async(char uplo, int n, int nrhs, T *a, int lda,              \
+                                           long long stride_a, T *b, int ldb, long long stride_b,  \
+                                           int nm, cbk_stream_t st)                                \
+    {                                                                                              \
+        return sym_solve_batched<T>(true, uplo, n, nrhs, a, lda, stride_a, b, ldb, stride_b, nm,   \
+                                    S(st));                                                        \
+    }                                                                                              \
+    int cbk_cuda_##P##gels_batched_async(char trans, int m, int n, int nrhs, T *a, int lda,        \
+                                         long long stride_a, T *b, int ldb, long long stride_b,    \
+                                         T *tau, int nm, cbk_stream_t st)                          \
+    {                                                                                              \
+        return gels_batched<T>(trans, m, n, nrhs, a, lda, stride_a, b, ldb, stride_b, tau, nm,     \
+                               S(st));                                                             \
+    }
+CBK_PLAIN_BATCHED(d, double)
+CBK_PLAIN_BATCHED(s, float)
+#undef CBK_PLAIN_BATCHED
 
 long long cbk_cuda_dposv_refined_compact_host_lwork(char layout, int n, int nrhs, int ldap,
                                                     int ldbp, int V, int nm)

@@ -128,11 +128,12 @@ bool chol_small_ok(int n)
 
 template <typename T>
 cudaError_t launch_chol_small(bool solve, bool row, bool up, int n, int nrhs, T *ap, int ldap,
-                              T *bp, int ldbp, int V, int nm, cudaStream_t s)
+                              T *bp, int ldbp, int V, int nm, cudaStream_t s, size_t sa_,
+                              size_t sb_)
 {
     const long ng = ((long)nm + V - 1) / V;
-    const size_t sa = gstride(row, ldap, n, n, V);
-    const size_t sb = solve ? gstride(row, ldbp, n, nrhs, V) : 0;
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, n, n, V);
+    const size_t sb = solve ? (sb_ ? sb_ : gstride(row, ldbp, n, nrhs, V)) : 0;
     const int th = std::min(threads_for(solve ? R_POSV : R_POTRF, n, sizeof(T)), 128);
     const unsigned bl = blocks_for(ng, V, th);
 #define CBK_CHOL_CASE(N)                                                                           \
@@ -154,8 +155,8 @@ cudaError_t launch_chol_small(bool solve, bool row, bool up, int n, int nrhs, T 
 }
 
 template cudaError_t launch_chol_small<float>(bool, bool, bool, int, int, float *, int, float *,
-                                              int, int, int, cudaStream_t);
+                                              int, int, int, cudaStream_t, size_t, size_t);
 template cudaError_t launch_chol_small<double>(bool, bool, bool, int, int, double *, int, double *,
-                                               int, int, int, cudaStream_t);
+                                               int, int, int, cudaStream_t, size_t, size_t);
 
 } // namespace cbkcuda

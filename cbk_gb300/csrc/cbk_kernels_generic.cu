@@ -126,12 +126,12 @@ cudaError_t launch_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, in
 
 template <typename T>
 cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, int V, int nm,
-                          cudaStream_t s)
+                          cudaStream_t s, size_t sa_)
 {
     const long ng = groups_of(nm, V);
-    const size_t sa = gstride(row, ldap, n, n, V);
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, n, n, V);
     if (!ldlt && chol_small_ok(n))
-        return launch_chol_small<T>(false, row, up, n, 0, ap, ldap, nullptr, 1, V, nm, s);
+        return launch_chol_small<T>(false, row, up, n, 0, ap, ldap, nullptr, 1, V, nm, s, sa);
     const int th = threads_for(ldlt ? R_SYTRFNP : R_POTRF, n, sizeof(T));
     if (ldlt)
         k_factor<T, true><<<blocks_for(ng, V, th), th, 0, s>>>(row, up, n, ap, ldap, V, ng, sa);
@@ -143,10 +143,11 @@ cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, 
 template <typename T>
 cudaError_t launch_sym_solve_generic(bool ldlt, bool fused, bool row, bool up, int n, int nrhs,
                                      T *ap, int ldap, T *bp, int ldbp, int V, int nm,
-                                     cudaStream_t s)
+                                     cudaStream_t s, size_t sa_ = 0, size_t sb_ = 0)
 {
     const long ng = groups_of(nm, V);
-    const size_t sa = gstride(row, ldap, n, n, V), sb = gstride(row, ldbp, n, nrhs, V);
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, n, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, n, nrhs, V);
     const int r = ldlt ? (fused ? R_SYSVNP : R_SYTRSNP) : (fused ? R_POSV : R_POTRS);
     const int th = threads_for(r, n, sizeof(T));
     const unsigned bl = blocks_for(ng, V, th);
@@ -221,39 +222,43 @@ cudaError_t launch_orgqr(bool row, int m, int n, int k, T *ap, int ldap, const T
 
 template <typename T>
 cudaError_t launch_gels(bool row, bool tran, int m, int n, int nrhs, T *ap, int ldap, T *bp,
-                        int ldbp, T *taup, int V, int nm, cudaStream_t s)
+                        int ldbp, T *taup, int V, int nm, cudaStream_t s, size_t sa_, size_t sb_)
 {
     const long ng = groups_of(nm, V);
     const bool tall = m >= n;
     const int p = tall ? m : n, q = tall ? n : m;
     const bool overdet = (tall != tran);
-    if (q == 0) return launch_zero<T>(row, p, nrhs, bp, ldbp, V, nm, s);
+    const size_t sa = sa_ ? sa_ : gstride(row, ldap, m, n, V);
+    const size_t sb = sb_ ? sb_ : gstride(row, ldbp, p, nrhs, V);
+    if (q == 0) return launch_zero<T>(row, p, nrhs, bp, ldbp, V, nm, s, sb);
     const int th = threads_for(R_GELS, p, sizeof(T));
     auto kern = p >= WY_MMIN ? k_gels<T, true> : k_gels<T, false>;
     kern<<<blocks_for(ng, V, th), th, 0, s>>>(row, tall, overdet, p, q, nrhs, ap, ldap, bp, ldbp,
-                                              taup, V, ng, gstride(row, ldap, m, n, V),
-                                              gstride(row, ldbp, p, nrhs, V), (size_t)q * V);
+                                              taup, V, ng, sa, sb, (size_t)q * V);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, int nrhs, T *ap,
-                             int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s)
+                             int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s,
+                             size_t sa_, size_t sb_)
 {
     if (!ldlt && fused && chol_small_ok(n))
-        return launch_chol_small<T>(true, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, s);
+        return launch_chol_small<T>(true, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm, s, sa_,
+                                    sb_);
     return launch_sym_solve_generic<T>(ldlt, fused, row, up, n, nrhs, ap, ldap, bp, ldbp, V, nm,
-                                       s);
+                                       s, sa_, sb_);
 }
 
 #define CBK_INSTANTIATE(T)                                                                        \
     template cudaError_t launch_zero<T>(bool, int, int, T *, int, int, int, cudaStream_t, size_t); \
     template cudaError_t launch_factor<T>(bool, bool, bool, int, T *, int, int, int,               \
-                                          cudaStream_t);                                          \
+                                          cudaStream_t, size_t);                                  \
     template cudaError_t launch_sym_solve_generic<T>(bool, bool, bool, bool, int, int, T *, int,   \
-                                                     T *, int, int, int, cudaStream_t);           \
+                                                     T *, int, int, int, cudaStream_t, size_t,    \
+                                                     size_t);                                     \
     template cudaError_t launch_sym_solve<T>(bool, bool, bool, bool, int, int, T *, int, T *, int, \
-                                             int, int, cudaStream_t);                             \
+                                             int, int, cudaStream_t, size_t, size_t);             \
     template cudaError_t launch_trsm<T>(bool, bool, bool, bool, bool, int, int, T, const T *, int, \
                                         T *, int, int, int, cudaStream_t);                        \
     template cudaError_t launch_geqrf<T>(bool, int, int, T *, int, T *, int, int, cudaStream_t);   \
@@ -262,7 +267,7 @@ cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, in
     template cudaError_t launch_orgqr<T>(bool, int, int, int, T *, int, const T *, int, int,       \
                                          cudaStream_t);                                           \
     template cudaError_t launch_gels<T>(bool, bool, int, int, int, T *, int, T *, int, T *, int,   \
-                                        int, cudaStream_t);
+                                        int, cudaStream_t, size_t, size_t);
 CBK_INSTANTIATE(float)
 CBK_INSTANTIATE(double)
 #undef CBK_INSTANTIATE

@@ -48,7 +48,7 @@ cudaError_t launch_zero(bool row, int rows, int cols, T *bp, int ldbp, int V, in
 // potrf (ldlt = false) / sytrfnp (ldlt = true) of the named triangle
 template <typename T>
 cudaError_t launch_factor(bool ldlt, bool row, bool up, int n, T *ap, int ldap, int V, int nm,
-                          cudaStream_t s);
+                          cudaStream_t s, size_t sa_ = 0);
 
 // Cholesky factor (+ solve when `solve`) of orders 1 .. CHOL_SMALL_NMAX with the
 // matrix in registers (cbk_kernels_chol_reg.cu): the generic kernels' bits
@@ -56,12 +56,16 @@ constexpr int CHOL_SMALL_NMAX = 8;
 bool chol_small_ok(int n);
 template <typename T>
 cudaError_t launch_chol_small(bool solve, bool row, bool up, int n, int nrhs, T *ap, int ldap,
-                              T *bp, int ldbp, int V, int nm, cudaStream_t s);
+                              T *bp, int ldbp, int V, int nm, cudaStream_t s, size_t sa_ = 0,
+                              size_t sb_ = 0);
 
-// potrs / posv (ldlt = false), sytrsnp / sysvnp (ldlt = true); fused = factor first
+// potrs / posv (ldlt = false), sytrsnp / sysvnp (ldlt = true); fused = factor first.
+// sa_ / sb_: group strides of A and B (0: the compact layout's); a strided
+// dense batch is the compact layout at V = 1 with the caller's strides
 template <typename T>
 cudaError_t launch_sym_solve(bool ldlt, bool fused, bool row, bool up, int n, int nrhs, T *ap,
-                             int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s);
+                             int ldap, T *bp, int ldbp, int V, int nm, cudaStream_t s,
+                             size_t sa_ = 0, size_t sb_ = 0);
 
 template <typename T>
 cudaError_t launch_trsm(bool left, bool up, bool row, bool tran, bool unit, int m, int n, T alpha,
@@ -81,7 +85,8 @@ cudaError_t launch_orgqr(bool row, int m, int n, int k, T *ap, int ldap, const T
 
 template <typename T>
 cudaError_t launch_gels(bool row, bool tran, int m, int n, int nrhs, T *ap, int ldap, T *bp,
-                        int ldbp, T *taup, int V, int nm, cudaStream_t s);
+                        int ldbp, T *taup, int V, int nm, cudaStream_t s, size_t sa_ = 0,
+                        size_t sb_ = 0);
 
 // dense batch (matrix idx at a + idx*stride, element (i,j) at i + j*lda
 // column-major or i*lda + j row-major) <-> compact; padded lanes get pad_diag

@@ -330,6 +330,39 @@ int cbk_cuda_dposv_refined_batched_async(char uplo, int n, int nrhs, double *a, 
                                          double *berr, void *work, long long lwork,
                                          cbk_stream_t stream);
 
+/* The plain drivers on strided dense batches, the layout of cuBLAS/cuSOLVER
+ * batched routines: matrix k's A is column-major at a + k*stride_a with
+ * leading dimension lda, its B at b + k*stride_b with leading dimension ldb.
+ * No reference entry point (the reference's callers pack into the compact
+ * layout first, tests/test_compact_util.hpp:468-531): the kernels read and
+ * write the dense arrays directly, and each matrix gets exactly the bits of
+ * the compact entry point (?posv_compact, ?sysvnp_compact, ?gels_compact).
+ * ?posv_batched / ?sysvnp_batched (the uplo triangle referenced; nrhs = 0
+ * still factors): 0, -1 uplo, -2 n, -3 nrhs, -5 lda < max(1,n),
+ * -6 stride_a < lda*n, -8 ldb < max(1,n), -9 stride_b < ldb*nrhs, -10 nm.
+ * ?gels_batched (trans 'N' or 'T'; A m x n, B max(m,n) x nrhs, the min(m,n)
+ * tau values of matrix k at tau + k*min(m,n)): 0, -1 trans, -2 m, -3 n,
+ * -4 nrhs, -6 lda < max(1,m), -7 stride_a < lda*n, -9 ldb < max(1,m,n),
+ * -10 stride_b < ldb*nrhs, -12 nm. Or CBK_CUDA_ERROR_BASE + a CUDA error. */
+int cbk_cuda_dposv_batched_async(char uplo, int n, int nrhs, double *a, int lda,
+                                 long long stride_a, double *b, int ldb, long long stride_b,
+                                 int nm, cbk_stream_t stream);
+int cbk_cuda_sposv_batched_async(char uplo, int n, int nrhs, float *a, int lda,
+                                 long long stride_a, float *b, int ldb, long long stride_b, int nm,
+                                 cbk_stream_t stream);
+int cbk_cuda_dsysvnp_batched_async(char uplo, int n, int nrhs, double *a, int lda,
+                                   long long stride_a, double *b, int ldb, long long stride_b,
+                                   int nm, cbk_stream_t stream);
+int cbk_cuda_ssysvnp_batched_async(char uplo, int n, int nrhs, float *a, int lda,
+                                   long long stride_a, float *b, int ldb, long long stride_b,
+                                   int nm, cbk_stream_t stream);
+int cbk_cuda_dgels_batched_async(char trans, int m, int n, int nrhs, double *a, int lda,
+                                 long long stride_a, double *b, int ldb, long long stride_b,
+                                 double *tau, int nm, cbk_stream_t stream);
+int cbk_cuda_sgels_batched_async(char trans, int m, int n, int nrhs, float *a, int lda,
+                                 long long stride_a, float *b, int ldb, long long stride_b,
+                                 float *tau, int nm, cbk_stream_t stream);
+
 /* The same solve on batches in HOST memory (ap, bp, iters, berr are host
  * pointers; pinned memory lets the copies overlap the solves). No reference
  * entry point: the reference's own calling convention -- every array on the

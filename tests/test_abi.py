@@ -206,6 +206,45 @@ def test_refined_gels_batched_argument_checks():
     assert cbk_gb300.dgels_refined_batched_lwork(-1, 1, 1, 1) == -1
 
 
+@pytest.mark.parametrize("p", ["d", "s"])
+@pytest.mark.parametrize("routine", ["posv", "sysvnp"])
+def test_plain_batched_argument_checks(p, routine):
+    """?posv_batched / ?sysvnp_batched on strided dense batches: -j in
+    argument order and the quick returns (CPU only: no device work)."""
+    import cbk_gb300
+    f = getattr(cbk_gb300, f"{p}{routine}_batched")
+    assert f("X", 8, 1, None, 8, 64, None, 8, 8, 10) == -1
+    assert f("L", -1, 1, None, 8, 64, None, 8, 8, 10) == -2
+    assert f("L", 8, -1, None, 8, 64, None, 8, 8, 10) == -3
+    assert f("L", 8, 1, None, 7, 64, None, 8, 8, 10) == -5
+    assert f("L", 8, 1, None, 8, 63, None, 8, 8, 10) == -6
+    assert f("L", 8, 1, None, 8, 64, None, 7, 8, 10) == -8
+    assert f("L", 8, 2, None, 8, 64, None, 8, 15, 10) == -9
+    assert f("L", 8, 1, None, 8, 64, None, 8, 8, -1) == -10
+    assert f("U", 0, 1, None, 1, 0, None, 1, 1, 10) == 0
+    assert f("L", 8, 1, None, 8, 64, None, 8, 8, 0) == 0
+
+
+@pytest.mark.parametrize("p", ["d", "s"])
+def test_plain_gels_batched_argument_checks(p):
+    """?gels_batched on strided dense batches: -j in argument order (B holds
+    max(m, n) rows) and the quick returns (CPU only: no device work)."""
+    import cbk_gb300
+    f = getattr(cbk_gb300, f"{p}gels_batched")
+    assert f("X", 8, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -1
+    assert f("N", -1, 4, 1, None, 8, 32, None, 8, 8, None, 10) == -2
+    assert f("N", 8, -1, 1, None, 8, 32, None, 8, 8, None, 10) == -3
+    assert f("N", 8, 4, -1, None, 8, 32, None, 8, 8, None, 10) == -4
+    assert f("N", 8, 4, 1, None, 7, 32, None, 8, 8, None, 10) == -6
+    assert f("N", 8, 4, 1, None, 8, 31, None, 8, 8, None, 10) == -7
+    assert f("T", 4, 8, 1, None, 4, 32, None, 4, 8, None, 10) == -9
+    assert f("N", 8, 4, 2, None, 8, 32, None, 8, 15, None, 10) == -10
+    assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, -1) == -12
+    assert f("N", 8, 4, 0, None, 8, 32, None, 8, 0, None, 10) == 0
+    assert f("N", 0, 0, 1, None, 1, 0, None, 1, 1, None, 10) == 0
+    assert f("N", 8, 4, 1, None, 8, 32, None, 8, 8, None, 0) == 0
+
+
 def _noalloc_fn():
     import ctypes
 
