@@ -20,6 +20,7 @@
 #include "cbk_launch.h"
 
 #include <algorithm>
+#include <cstdint>
 #include <cuda_runtime.h>
 
 namespace cbkcuda {
@@ -94,12 +95,15 @@ cudaError_t posv_refined_host(bool row, bool up, int n, int nrhs, double *ap, in
     const Plan p = plan(row, n, nrhs, ldap, ldbp, V, nm);
     char *const ha = reinterpret_cast<char *>(ap);
     char *const hb = reinterpret_cast<char *>(bp);
-    // pinned (or registered) A: the device address the triangle kernel reads
+    // pinned (or registered) A, 16-byte aligned: the device address the
+    // triangle kernel reads with 16-byte moves (every chunk starts a whole
+    // number of groups on, a multiple of 16 bytes since V is even); an A
+    // that is only 8-byte aligned goes by the copy engine
     double *zc = nullptr;
     {
         cudaPointerAttributes at{};
         if (cudaPointerGetAttributes(&at, ap) == cudaSuccess && at.type == cudaMemoryTypeHost &&
-            at.devicePointer != nullptr)
+            at.devicePointer != nullptr && reinterpret_cast<uintptr_t>(at.devicePointer) % 16 == 0)
             zc = static_cast<double *>(at.devicePointer);
         cudaGetLastError(); // a pageable pointer is not an error
     }

@@ -98,3 +98,49 @@ def test_host_entry_argument_checks_and_workspace(cuda):
     assert need > 0
     assert f("C", "L", 48, 1, None, 48, None, 48, 32, 9000, dwork=0, lwork=need - 1) == -15
     assert f("C", "L", 0, 1, None, 1, None, 1, 32, 64, dwork=0, lwork=0) == 0
+
+
+def _pinned(a, offset):
+    """A pinned copy of a, starting `offset` doubles into its allocation."""
+    import torch
+    big = torch.empty(a.size + offset, dtype=torch.float64).pin_memory()
+    view = big[offset:]
+    view.copy_(torch.from_numpy(a))
+    return view
+
+
+@pytest.mark.parametrize("a_kind,b_kind", [("pinned", "pageable"), ("pinned+8", "pinned"),
+                                           ("pinned", "pinned+8"), ("pinned", "pinned")])
+def test_host_entry_mixed_memory_kinds(a_kind, b_kind, cuda):
+    """Every combination of pinned, pageable and pinned-but-only-8-byte-aligned
+    A and B gives the device entry point's bits. The device reads a pinned,
+    16-byte aligned A's triangle with 16-byte moves; a pinned A that is only
+    8-byte aligned goes by the copy engine, as a pageable one does."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(77)
+    n, nm, nrhs, V = 16, 12000, 1, 32
+    A, B = _batch(rng, nm, n, nrhs, fallbacks=True)
+    ap = O.pack(A, V, n)
+    bp = O.pack(B, V, n, pad_diag=0.0)
+    dap, dbp = torch.from_numpy(ap).cuda(), torch.from_numpy(bp).cuda()
+    dit = torch.full((nm,), -99, dtype=torch.int32, device="cuda")
+    assert cbk_gb300.dposv_refined_compact("C", "L", n, nrhs, dap, n, dbp, n, V, nm,
+                                           iters=dit) == 0
+    torch.cuda.synchronize()
+
+    def host(a, kind):
+        if kind == "pageable":
+            return a.copy()
+        return _pinned(a, 1 if kind.endswith("+8") else 0)
+    hap, hbp = host(ap, a_kind), host(bp, b_kind)
+    hit = np.full(nm, -99, dtype=np.int32)
+    assert cbk_gb300.dposv_refined_compact_host("C", "L", n, nrhs, hap, n, hbp, n, V, nm,
+                                                iters=hit) == 0
+    as_np = (lambda t: t) if isinstance(hap, np.ndarray) else (lambda t: t.numpy())
+    as_npb = (lambda t: t) if isinstance(hbp, np.ndarray) else (lambda t: t.numpy())
+    assert _same(as_np(hap), dap.cpu().numpy())
+    assert _same(as_npb(hbp), dbp.cpu().numpy())
+    assert _same(hit, dit.cpu().numpy())
+    assert hit[1] == -2
