@@ -28,12 +28,17 @@ namespace cbkcuda {
 namespace {
 
 constexpr int NBUF = 3;
-// A chunk moves about CHUNK_BYTES over the link (A's triangle and B), so its
-// copy outlasts the host's few calls per chunk; it holds at least
-// MIN_CHUNK_GROUPS groups, so its solve fills the GPU. The first and the
-// last chunk are a quarter of that (at least MIN_RAMP_GROUPS): the first
-// solve starts after a short copy, and the last copy leaves a short solve.
-constexpr size_t CHUNK_BYTES = (size_t)48 << 20;
+// A chunk moves about CHUNK_BYTES over the link (A's triangle and B), and
+// holds at least MIN_CHUNK_GROUPS groups, so its solve fills the GPU. Each
+// chunk costs the copy stream some tens of microseconds beyond its bytes
+// (launch, the copy kernel's tail, the DMA of B), so chunks are large:
+// measured at 262,144 matrices, 192 MiB chunks took n = 32 from 6.51 to
+// 6.31 ms and n = 48 from 13.3 to 13.0 ms against 48 MiB ones. The first and
+// the last chunk move about RAMP_BYTES (at least MIN_RAMP_GROUPS groups): the
+// first solve starts after a short copy, and the last copy leaves a short
+// solve.
+constexpr size_t CHUNK_BYTES = (size_t)192 << 20;
+constexpr size_t RAMP_BYTES = (size_t)12 << 20;
 constexpr long MIN_CHUNK_GROUPS = 256;
 constexpr long MIN_RAMP_GROUPS = 64;
 
@@ -68,7 +73,7 @@ Plan plan(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm)
     const size_t moved = (size_t)n * (n + 1) / 2 * V * sizeof(double) + p.gb;
     const long want = (long)((CHUNK_BYTES + moved - 1) / moved);
     p.chunk = std::min(p.ngroups, std::max(MIN_CHUNK_GROUPS, want));
-    p.ramp = std::min(p.chunk, std::max(MIN_RAMP_GROUPS, p.chunk / 4));
+    p.ramp = std::min(p.chunk, std::max(MIN_RAMP_GROUPS, (long)((RAMP_BYTES + moved - 1) / moved)));
     const size_t lanes = (size_t)p.chunk * V;
     p.a = align256(p.chunk * p.ga);
     p.b = align256(p.chunk * p.gb);

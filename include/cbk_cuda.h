@@ -367,8 +367,8 @@ int cbk_cuda_sgels_batched_async(char trans, int m, int n, int nrhs, float *a, i
  * pointers; pinned memory lets the copies overlap the solves). No reference
  * entry point: the reference's own calling convention -- every array on the
  * host, as in ?posv_compact (include/cbk.h:196-212) -- over the device solve
- * above. The batch is cut into chunks of whole groups (about 48 MiB of
- * input each, at least 256 groups; the first and last a quarter of that)
+ * above. The batch is cut into chunks of whole groups (about 192 MiB of
+ * input each, at least 256 groups; the first and last about 12 MiB)
  * that pass through three device slots on three streams, so that copying one
  * chunk in, solving another and copying a third out overlap. The workspace
  * is therefore bounded whatever nm. When ap is pinned (or registered)

@@ -153,10 +153,11 @@ def test_refined_host_entry_validates_before_any_device_work():
     assert lw("C", 48, 1, 48, 48, 32, 64) >= 3 * 32 * 48 * 48 * 8
     assert lw("C", 48, 1, 50, 48, 32, 64) > lw("C", 48, 1, 48, 48, 32, 64)
     assert lw("C", 48, 1, 48, 48, 32, 10 ** 3) < lw("C", 48, 1, 48, 48, 32, 10 ** 5)
-    # chunks are sized by bytes moved: the workspace stops growing with nm
+    # chunks are sized by bytes moved (about 192 MiB of A's triangle and B,
+    # 643 groups at n = 48): the workspace stops growing with nm
     big = lw("C", 48, 1, 48, 48, 32, 10 ** 6)
     assert big == lw("C", 48, 1, 48, 48, 32, 2 * 10 ** 6)
-    assert big < 3 * 300 * 32 * 48 * 48 * 8 + (64 << 20)
+    assert big < 3 * 700 * 32 * 48 * 48 * 8 + (64 << 20)
     assert lw("C", 8, 1, 8, 8, 32, 10 ** 7) == lw("C", 8, 1, 8, 8, 32, 2 * 10 ** 7)
 
 
