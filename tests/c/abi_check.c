@@ -50,6 +50,18 @@ int main(void)
                                                 0, 0, 0),
            -17);
     EXPECT(cbk_cuda_dgels_refined_batched_lwork(-1, 1, 1, 1), -1);
+    /* the plain drivers on strided dense batches, both precisions */
+    {
+        float fa[4] = {0}, fb[4] = {0}, ft[4] = {0};
+        EXPECT(cbk_cuda_dposv_batched_async('X', 8, 1, a, 8, 64, b, 8, 8, 10, 0), -1);
+        EXPECT(cbk_cuda_dposv_batched_async('L', 8, 1, a, 8, 63, b, 8, 8, 10, 0), -6);
+        EXPECT(cbk_cuda_sposv_batched_async('U', 8, 2, fa, 8, 64, fb, 8, 15, 10, 0), -9);
+        EXPECT(cbk_cuda_dsysvnp_batched_async('L', 8, 1, a, 8, 64, b, 7, 8, 10, 0), -8);
+        EXPECT(cbk_cuda_ssysvnp_batched_async('L', 0, 1, fa, 1, 0, fb, 1, 1, 10, 0), 0);
+        EXPECT(cbk_cuda_dgels_batched_async('N', 8, 4, 1, a, 8, 31, b, 8, 8, t, 10, 0), -7);
+        EXPECT(cbk_cuda_sgels_batched_async('T', 4, 8, 1, fa, 4, 32, fb, 4, 8, ft, 10, 0), -9);
+        EXPECT(cbk_cuda_sgels_batched_async('N', 8, 4, 1, fa, 8, 32, fb, 8, 8, ft, -1, 0), -12);
+    }
     if (fails == 0) printf("c abi ok\n");
     return fails != 0;
 }
