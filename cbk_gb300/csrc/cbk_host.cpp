@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 namespace cbkcuda {
@@ -74,6 +75,16 @@ Plan plan(bool row, int n, int nrhs, int ldap, int ldbp, int V, int nm)
     const long want = (long)((CHUNK_BYTES + moved - 1) / moved);
     p.chunk = std::min(p.ngroups, std::max(MIN_CHUNK_GROUPS, want));
     p.ramp = std::min(p.chunk, std::max(MIN_RAMP_GROUPS, (long)((RAMP_BYTES + moved - 1) / moved)));
+    // CBK_CUDA_HOST_CHUNK_GROUPS=g (read on every call, and by the workspace
+    // query): chunks of g groups, the first and last g / 4 -- for tests of
+    // the pipeline's chunking on small batches, or a caller's own tuning
+    if (const char *e = std::getenv("CBK_CUDA_HOST_CHUNK_GROUPS")) {
+        const long g = std::strtol(e, nullptr, 10);
+        if (g > 0) {
+            p.chunk = std::min(p.ngroups, g);
+            p.ramp = std::min(p.chunk, std::max(1L, g / 4));
+        }
+    }
     const size_t lanes = (size_t)p.chunk * V;
     p.a = align256(p.chunk * p.ga);
     p.b = align256(p.chunk * p.gb);

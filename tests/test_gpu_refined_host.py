@@ -144,3 +144,22 @@ def test_host_entry_mixed_memory_kinds(a_kind, b_kind, cuda):
     assert _same(as_npb(hbp), dbp.cpu().numpy())
     assert _same(hit, dit.cpu().numpy())
     assert hit[1] == -2
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_entry_many_chunks(pinned, cuda, monkeypatch):
+    """A batch cut into many small chunks (CBK_CUDA_HOST_CHUNK_GROUPS): every
+    device slot is reused several times, and chunks past the first hold lanes
+    that fall back (their A comes back as the FP64 factor) -- still the device
+    entry point's bits."""
+    monkeypatch.setenv("CBK_CUDA_HOST_CHUNK_GROUPS", "5")
+    rng = np.random.default_rng(5)
+    n, nm, nrhs, V = 16, 32 * 37 + 7, 2, 32      # 38 groups: chunks of 1, 5, .., 5, 1
+    A, B = _batch(rng, nm, n, nrhs, fallbacks=True)
+    A[700] *= 1e42                      # group 21: iters -2
+    A[1100, 3, 3] = np.nan              # group 34: iters -3
+    dev, host = _both(A, B, "C", "L", V, n + 1, n, pinned=pinned)
+    for name, d, h in zip(("ap", "bp", "iters", "berr"), dev, host):
+        assert _same(d, h), name
+    it = host[2]
+    assert it[1] == -2 and it[700] == -2 and it[1100] < 0
