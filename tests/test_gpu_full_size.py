@@ -2,9 +2,9 @@
 properties that hold at any size: backward errors and the normal equations
 within their bounds, orthogonality, every refined matrix converged, and the
 bit-identities the library promises -- fused == separate, dense batches ==
-the compact layout, bucketed == one call per order. At these sizes the
-offsets into the batch pass 2^31 elements, which the small parity cases never
-reach. Inputs are made on the device from seeds (orthogonal factors by this
+the compact layout, bucketed == one call per order. At these sizes byte
+offsets into the batch pass 2^31 (A at n = 48: 4.8 GB), which the small
+parity cases never reach. Inputs are made on the device from seeds (orthogonal factors by this
 library's own dgeqrf/dorgqr); every check runs on the device in FP64.
 """
 import pytest
