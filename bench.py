@@ -816,7 +816,10 @@ def e2e(args, cbk, batches, barrier, ws):
     # then overlap on the host link: 21.5 against 22.4 ms for the calls one
     # after another, with the same bits.
     from concurrent.futures import ThreadPoolExecutor
-    pool = ThreadPoolExecutor(len(host))
+    dev = batches[0]["ap"].device
+    # each worker makes this rank's GPU its current device (a new thread
+    # starts on device 0; the library runs on the caller's current device)
+    pool = ThreadPoolExecutor(len(host), initializer=torch.cuda.set_device, initargs=(dev,))
     by_size = sorted(host, key=lambda h: -h["n"])
 
     def call(h):
