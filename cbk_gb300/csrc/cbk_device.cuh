@@ -15,7 +15,8 @@
 // the branch-free larfg, dlarf sweeps, org2r), restated for one lane:
 //  * factorizations are blocked left-looking by 8-column panels: a panel's
 //    columns first take the whole rank-j0 update from the finished columns in
-//    pivot order (4 x 8 register tiles), then the in-panel rank-1 sweep --
+//    pivot order (4 x 8 register tiles), then the in-panel rank-1 sweep
+//    (each row below the panel's diagonal block in registers) --
 //    the same per-element operation sequence as the reference's recursion
 //    (src/cbk_potrf_compact.hpp:79-124, src/cbk_sytrfnp_compact.hpp:96-254);
 //  * the FP64 pipe of a GB300 SM retires about two FMAs per clock, so each
@@ -433,6 +434,99 @@ __device__ void cross_panel_update(int n, LV<T> A, int j0, int j1)
     }
 }
 
+// The unblocked sweep of the NC panel columns j0 .. j0+NC-1 (already updated
+// by the columns left of them), per pivot j: the weight 1/a, the rank-1 step
+// on the unscaled column A(i,q) -= A(i,j) * (A(q,j) / a) for the panel columns
+// q > j, then the sqrt and the column scaling off the pivot-to-pivot chain
+// (src/cbk_potrf_compact.hpp:79-105; src/cbk_sytrfnp_compact.hpp:96-112,
+// 216-235). The NC x NC diagonal block is swept in place first, leaving the
+// weights w(j, q) = A(q,j) / a_j and the column scales in registers; every
+// row below it is then carried through all NC pivots in registers, with the
+// same operations in the same order, so each of its elements is read and
+// written once instead of once per pivot (a lane's matrix does not fit in L1
+// from order 32 on: those passes went to L2 or DRAM, and took a quarter of
+// the time of posv at n = 16 .. 48).
+template <typename T, bool LDLT, int NC>
+__device__ void panel_sweep_nc(int n, LV<T> A, int j0)
+{
+    constexpr int NW = NC * (NC - 1) / 2 > 0 ? NC * (NC - 1) / 2 : 1;
+    T w[NW];   // w(j, q) at j (2 NC - j - 1) / 2 + (q - j - 1), q > j
+    T scl[NC]; // the column scales
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const T a = A(j0 + j, j0 + j);
+        const bool pos = !LDLT && a > T(0) && a <= FLT_OR_DBL_MAX<T>();
+        T inva, rs = T(0);
+        if (pos) {
+            rs = rsqrt(a);
+            inva = rs * rs;
+        }
+        else {
+            inva = rcp(a);
+        }
+#pragma unroll
+        for (int q = j + 1; q < NC; ++q)
+            w[j * (2 * NC - j - 1) / 2 + (q - j - 1)] = A(j0 + q, j0 + j) * inva;
+#pragma unroll
+        for (int r = j + 1; r < NC; ++r) {
+            const T aij = A(j0 + r, j0 + j);
+#pragma unroll
+            for (int q = j + 1; q <= r; ++q)
+                A(j0 + r, j0 + q) =
+                    fma(-aij, w[j * (2 * NC - j - 1) / 2 + (q - j - 1)], A(j0 + r, j0 + q));
+        }
+        T scale;
+        if (LDLT) {
+            scale = inva;
+        }
+        else if (pos) {
+            A(j0 + j, j0 + j) = a * rs;
+            scale = rs;
+        }
+        else {
+            const T s = sqrt(a);
+            A(j0 + j, j0 + j) = s;
+            scale = s * inva;
+        }
+        scl[j] = scale;
+#pragma unroll
+        for (int r = j + 1; r < NC; ++r)
+            A(j0 + r, j0 + j) = A(j0 + r, j0 + j) * scale;
+    }
+    // the rows below the block, one at a time
+    for (int i = j0 + NC; i < n; ++i) {
+        T x[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+            x[c] = A(i, j0 + c);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            const T aij = x[j];
+#pragma unroll
+            for (int q = j + 1; q < NC; ++q)
+                x[q] = fma(-aij, w[j * (2 * NC - j - 1) / 2 + (q - j - 1)], x[q]);
+            x[j] = x[j] * scl[j];
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+            A(i, j0 + c) = x[c];
+    }
+}
+
+template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int j0, int j1)
+{
+    switch (j1 - j0) {
+    case 8: panel_sweep_nc<T, LDLT, 8>(n, A, j0); break;
+    case 7: panel_sweep_nc<T, LDLT, 7>(n, A, j0); break;
+    case 6: panel_sweep_nc<T, LDLT, 6>(n, A, j0); break;
+    case 5: panel_sweep_nc<T, LDLT, 5>(n, A, j0); break;
+    case 4: panel_sweep_nc<T, LDLT, 4>(n, A, j0); break;
+    case 3: panel_sweep_nc<T, LDLT, 3>(n, A, j0); break;
+    case 2: panel_sweep_nc<T, LDLT, 2>(n, A, j0); break;
+    default: panel_sweep_nc<T, LDLT, 1>(n, A, j0); break;
+    }
+}
+
 // The in-panel rank-1 step of pivot j on the NQ panel columns to its right,
 // on the unscaled column with the weight 1/a (sytrfnp_update_block,
 // src/cbk_sytrfnp_compact.hpp:96-112): A(i,c) -= A(i,j) * (A(c,j) / a),
@@ -459,11 +553,11 @@ template <typename T, int NQ> __device__ void rank1_panel(int n, LV<T> A, int j,
     }
 }
 
-// The unblocked sweep of panel j0 .. j1-1 (already updated by the columns
-// left of it): per pivot the reciprocal, the in-panel rank-1 step, then the
-// sqrt and the column scaling off the pivot-to-pivot chain
-// (src/cbk_potrf_compact.hpp:79-105; src/cbk_sytrfnp_compact.hpp:216-235).
-template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int j0, int j1)
+// panel_sweep's operations in the same order, each pivot's step applied to
+// the panel in memory: slower from order 16 on, but it keeps no weights in
+// registers, for a caller whose registers are spoken for (the FP64 fallback
+// inlined in the refined warp kernel).
+template <typename T, bool LDLT> __device__ void panel_sweep_mem(int n, LV<T> A, int j0, int j1)
 {
     for (int j = j0; j < j1; ++j) {
         const T a = A(j, j);
@@ -508,12 +602,16 @@ template <typename T, bool LDLT> __device__ void panel_sweep(int n, LV<T> A, int
     }
 }
 
-template <typename T, bool LDLT> __device__ void factor_lane(int n, LV<T> A)
+// MEM: the panel sweep in memory (panel_sweep_mem; the same bits)
+template <typename T, bool LDLT, bool MEM = false> __device__ void factor_lane(int n, LV<T> A)
 {
     for (int j0 = 0; j0 < n; j0 += 8) {
         const int j1 = min(j0 + 8, n);
         if (j0 > 0) cross_panel_update<T, LDLT>(n, A, j0, j1);
-        panel_sweep<T, LDLT>(n, A, j0, j1);
+        if (MEM)
+            panel_sweep_mem<T, LDLT>(n, A, j0, j1);
+        else
+            panel_sweep<T, LDLT>(n, A, j0, j1);
     }
 }
 

@@ -60,7 +60,10 @@ __global__ void __launch_bounds__(128) k_bucketed(const __grid_constant__ Bucket
         const int v = (int)(l - g * V);
         LV<T> A = lv_make<T>(tab.ap[b] + g * tab.sa[b] + v, row, tab.ldap[b], V, n, n);
         if (up) A = A.t();
-        factor_lane<T, LDLT>(n, A);
+        // FP32: the in-memory panel sweep (the same bits), which keeps this
+        // kernel at its former 128 registers (the register sweep took it to
+        // 168 with spills in the Cholesky instance)
+        factor_lane<T, LDLT, sizeof(T) == 4>(n, A);
         if (nrhs > 0)
             sym_solve_lane<T, LDLT>(n, nrhs, A,
                                     lv_make<T>(tab.bp[b] + g * tab.sb[b] + v, row, tab.ldbp[b], V, n, nrhs));

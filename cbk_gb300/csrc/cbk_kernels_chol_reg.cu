@@ -6,7 +6,7 @@
 // and solved there, and stored once: the generic kernel keeps the factor in
 // global memory and waits on a load at every step of its dependency chain.
 // The arithmetic is the generic kernels', operation for operation, in the
-// same order (cbk_device.cuh: panel_sweep / rank1_panel for a single 8-column
+// same order (cbk_device.cuh: panel_sweep_nc for a single 8-column
 // panel, then sym_solve_lane), so potrf and posv here give exactly the bits
 // of the generic potrf and potrs -- fused == separate holds whichever kernel
 // runs. (The reference: src/cbk_potrf_compact.hpp:79-105 for the panel,
@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(128)
         for (int i = j; i < N; ++i)
             a[i][j] = A(i, j);
     // pivot j: the weight 1/a, the rank-1 step on the unscaled column, then the
-    // diagonal and the column scale (panel_sweep with rank1_panel<N-1-j>)
+    // diagonal and the column scale (panel_sweep_nc's diagonal block)
 #pragma unroll
     for (int j = 0; j < N; ++j) {
         const T ajj = a[j][j];

@@ -169,7 +169,7 @@ struct WarpOut {
 // factor in local memory for the whole kernel.
 __device__ __forceinline__ void warp_fallback(int n, int nrhs, int first, LV<double> A, LV<double> B)
 {
-    factor_lane<double, false>(n, A);
+    factor_lane<double, false, true>(n, A); // the in-memory sweep: the kernel's registers are spoken for
     if (first < nrhs) {
         const LV<double> Bs = lv_from_col(B, first);
         sym_solve_lane<double, false>(n, nrhs - first, A, Bs);
