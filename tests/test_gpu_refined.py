@@ -244,3 +244,32 @@ def test_refined_batched_edges(n, nrhs, nm, cuda):
     bh = bd.cpu().numpy()
     Xd = np.stack([bh[k * sb:k * sb + nrhs * ldb].reshape(nrhs, ldb)[:, :n].T for k in range(nm)])
     assert np.array_equal(Xd, X) and np.array_equal(itd.cpu().numpy(), it)
+
+
+@pytest.mark.parametrize("n", [16, 24, 40, 48, 64, 70])
+def test_forced_fallback_is_the_plain_factor(n, cuda):
+    """Matrices scaled past the FP32 range fall back (iters -2) in every
+    kernel -- the lane kernel (16), the warp kernel (24 .. 64, whose inlined
+    fallback sweeps its panels in memory) and the workspace kernel (70) --
+    and hold exactly dpotrf_compact's factor (whose panel sweep keeps each
+    row in registers) and the plain solve's x."""
+    import torch
+
+    import cbk_gb300
+    rng = np.random.default_rng(400 + n)
+    nm, V = 96, 32
+    A, _ = C.gen_spd_cond(rng, nm, n)
+    big = np.arange(0, nm, 7)
+    A[big] *= 1e42
+    B = rng.standard_normal((nm, n, 1))
+    info, X, a1, a0, it, be = _run(A, B, V)
+    assert info == 0 and (it[big] == -2).all()
+    F = O.unpack(_plain_factor(A, V), nm, n, n, V, n)
+    A1 = O.unpack(a1, nm, n, n, V, n)
+    assert np.array_equal(F[big].view(np.uint64), A1[big].view(np.uint64))
+    ap = torch.from_numpy(O.pack(A, V, n)).cuda()
+    bp = torch.from_numpy(O.pack(B, V, n, pad_diag=0.0)).cuda()
+    assert cbk_gb300.dposv_compact("C", "L", n, 1, ap, n, bp, n, V, nm) == 0
+    torch.cuda.synchronize()
+    Xp = O.unpack(bp.cpu().numpy(), nm, n, 1, V, n)
+    assert np.array_equal(Xp[big].view(np.uint64), X[big].view(np.uint64))
