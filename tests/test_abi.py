@@ -342,3 +342,21 @@ def test_host_layer_workspace_query_and_codes():
     assert H.call(np.float32, "gels", ["C", "N", 16, 8, 4, None, 16, None, 16, None, 32, 40],
                   None, lw) == 0
     assert lw.value == 2 * 16 * 8 * 32 * 4 + 2 * 16 * 4 * 32 * 4 + 2 * 8 * 32 * 4
+
+
+def test_host_chunk_override_in_the_size_query(monkeypatch):
+    """CBK_CUDA_HOST_CHUNK_GROUPS sets the host pipeline's chunk (in groups),
+    read by the workspace query as by the call: three slots of g groups; an
+    unset, zero or unparsable value keeps the default chunking."""
+    import cbk_gb300
+    lw = cbk_gb300.dposv_refined_host_lwork
+    monkeypatch.delenv("CBK_CUDA_HOST_CHUNK_GROUPS", raising=False)
+    default = lw("C", 16, 1, 16, 16, 32, 32 * 1000)
+    monkeypatch.setenv("CBK_CUDA_HOST_CHUNK_GROUPS", "5")
+    five = lw("C", 16, 1, 16, 16, 32, 32 * 1000)
+    monkeypatch.setenv("CBK_CUDA_HOST_CHUNK_GROUPS", "10")
+    ten = lw("C", 16, 1, 16, 16, 32, 32 * 1000)
+    assert 0 < five < ten < default
+    for bad in ("0", "-3", "chunks"):
+        monkeypatch.setenv("CBK_CUDA_HOST_CHUNK_GROUPS", bad)
+        assert lw("C", 16, 1, 16, 16, 32, 32 * 1000) == default
